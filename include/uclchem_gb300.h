@@ -1,0 +1,164 @@
+/*
+ * uclchem_gb300 — C ABI of the GB300 batched chemistry solver.
+ *
+ * This is the drop-in seam for UCLCHEM's chemistry integration hot path: the
+ * calls that UCLCHEM's Fortran makes inside updateChemistry /
+ * integrateODESystem (rate coefficients, the generated RHS, DVODE) are
+ * replaced by batched calls that run many grid points at once on one GPU.
+ *
+ * Conventions
+ *  - plain C types only; every array is caller-owned host memory unless the
+ *    name says "_dev" (device pointer, caller-owned, on the context's device);
+ *  - abundance vectors are NEQ = nspec+1 doubles (species then density), the
+ *    layout of abund(:,dstep) in src/fortran_src/chemistry.f90:40;
+ *  - batched arrays are system-major: system s occupies [s*NEQ, (s+1)*NEQ);
+ *  - every function returns 0 on success or a negative UCL_E_* code, never
+ *    aborts; per-system status words reuse UCLCHEM/DVODE numbering;
+ *  - one context per host thread; calls on one context are serialised; each
+ *    context owns one CUDA stream.
+ */
+#ifndef UCLCHEM_GB300_H
+#define UCLCHEM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Error codes (library level).                                              */
+#define UCL_OK 0
+#define UCL_E_ARG (-101)      /* invalid argument / size                     */
+#define UCL_E_CUDA (-102)     /* CUDA runtime error                          */
+#define UCL_E_NOMEM (-103)    /* device allocation failed / over budget      */
+#define UCL_E_NET (-104)      /* network file unreadable or inconsistent     */
+#define UCL_E_UNSUPPORTED (-105) /* option outside the supported path        */
+#define UCL_E_TIMEOUT (-106)  /* a bounded device wait expired               */
+
+/* Per-model status words: UCLCHEM's error codes, constants.f90:22-27. */
+#define UCL_PARAMETER_READ_ERROR (-1)
+#define UCL_PHYSICS_INIT_ERROR (-2)
+#define UCL_CHEM_INIT_ERROR (-3)
+#define UCL_INT_UNRECOVERABLE_ERROR (-4)
+#define UCL_INT_TOO_MANY_FAILS_ERROR (-5)
+#define UCL_NOT_ENOUGH_TIMEPOINTS_ERROR (-6)
+
+/* Number of physics columns per output row (io.f90:74-81):
+ * time [yr], density, gasTemp, dustTemp, Av, radfield, zeta, point. */
+#define UCL_N_PHYS 8
+
+/* ------------------------------------------------------------------------ */
+/* Model parameters: the fields of UCLCHEM's parameter dictionary that the
+ * chemistry path reads (src/fortran_src/defaultparameters.f90:18-119).
+ * Defaults (including the single-precision rounding of the reference's
+ * default-REAL literals) are filled by ucl_params_default().               */
+typedef struct ucl_model_params {
+  double initialTemp, initialDens, finalDens, finalTime;
+  double radfield, zeta, rout, rin, baseAv;
+  double freezeFactor, freefallFactor;
+  double metallicity;
+  double fh, fhe, fc, fo, fn, fs, fmg, fsi, fcl, fp, ff, fd, fli, fna, fpah,
+      f15n, f13c, f18o;
+  double reltol, abstol_factor, abstol_min;
+  double ebmaxh2, ebmaxcr, ebmaxuvcr, epsilon, uv_yield, phi, uvcreff, omega;
+  int32_t freefall, endAtFinalDensity;
+  int32_t desorb, h2desorb, crdesorb, uvdesorb, thermdesorb;
+  int32_t ion, points, mxstep;
+  int32_t enforceChargeConservation, improvedH2CRPDissociation;
+} ucl_model_params;
+
+/* Fill *p with the reference defaults (defaultparameters.f90:18-119). */
+void ucl_params_default(ucl_model_params* p);
+
+/* ------------------------------------------------------------------------ */
+/* Network tables (compiled from MakeRates' network.f90 + odes.f90).         */
+typedef struct ucl_network ucl_network;
+
+/* Load a compiled network blob ("UCLNET01", written by
+ * uclchem_gb300/network.py).  Replaces the compile-time PARAMETER arrays of
+ * src/fortran_src/network.f90:4-5169 and the generated odes.f90. */
+int ucl_network_load(const char* path, ucl_network** out);
+void ucl_network_free(ucl_network* net);
+int ucl_network_nspec(const ucl_network* net);
+int ucl_network_nreac(const ucl_network* net);
+
+/* ------------------------------------------------------------------------ */
+/* Context: device tables + workspace on one GPU.                            */
+typedef struct ucl_ctx ucl_ctx;
+
+/* Solver precision for the Newton matrix: FP64 LU (plain path) or FP32 LU
+ * of the error-weight-equilibrated matrix refined by the FP64 Newton
+ * iteration (mixed path).  Rates, RHS, Nordsieck history, error norms and
+ * step control are FP64 in both. */
+#define UCL_PREC_FP64 0
+#define UCL_PREC_MIXED 1
+
+/* Create a context on CUDA device `device` for network `net` (copied to the
+ * device).  `hbm_budget` bounds the bytes of per-system workspace the
+ * context may hold (0 = library default).  Replaces the one-time set-up of
+ * initializeChemistry (src/fortran_src/chemistry.f90:46-141). */
+int ucl_ctx_create(const ucl_network* net, int device, size_t hbm_budget,
+                   ucl_ctx** out);
+void ucl_ctx_destroy(ucl_ctx* ctx);
+
+/* Rate coefficients for `nsys` systems.  Replaces calculateReactionRates
+ * (src/fortran_src/rates.f90:21-343) as called from updateChemistry
+ * (chemistry.f90:179-203): the surface/bulk totals of abund are refreshed
+ * (chemistry.f90:192-199) before the rates are evaluated.
+ *   params   [nsys]           model parameters
+ *   abund    [nsys*NEQ]       abundances + density (in/out: totals refreshed)
+ *   av       [nsys]           visual extinction of each system
+ *   phi      [nsys]           CR-desorption yield state (in/out, see DESIGN)
+ *   rates    [nsys*nreac]     out */
+int ucl_rates_batch(ucl_ctx* ctx, int nsys, const ucl_model_params* params,
+                    double* abund, const double* av, double* phi,
+                    double* rates);
+
+/* Right-hand side F(t, y) for `nsys` systems.  Replaces F / GETYDOT
+ * (src/fortran_src/chemistry.f90:294-352, odes.f90:6-5181).  The H2 and CO
+ * photodissociation rates are re-evaluated from y as F does
+ * (chemistry.f90:315-318); `rates` is not modified.
+ *   y     [nsys*NEQ], rates [nsys*nreac], av [nsys], ydot [nsys*NEQ] out */
+int ucl_rhs_batch(ucl_ctx* ctx, int nsys, const ucl_model_params* params,
+                  const double* y, const double* rates, const double* av,
+                  double* ydot);
+
+/* Analytic Jacobian dF/dy for `nsys` systems, dense column-major NEQ x NEQ
+ * per system (the matrix DVODE's MITER=2 branch approximates by finite
+ * differences, dvode.f90:8331-8355).  jac [nsys*NEQ*NEQ] out. */
+int ucl_jac_batch(ucl_ctx* ctx, int nsys, const ucl_model_params* params,
+                  const double* y, const double* rates, const double* av,
+                  double* jac);
+
+/* Per-model results of a whole run. */
+typedef struct ucl_model_stats {
+  int64_t nst, nfe, nje, nlu, nni, ncfn, netf; /* DVODE counters, summed   */
+  int32_t n_intervals, n_retries;              /* output rows, retry loops  */
+  double solve_ms;                              /* device latency of model  */
+} ucl_model_stats;
+
+/* Integrate whole CLOUD models on the device, one output row per interval
+ * of the reference schedule (cloud.f90:39-51), with the reference's retry
+ * and failure logic (chemistry.f90:145-292) and output layout
+ * (io.f90:74-82).  Replaces the time loop of solveAbundances
+ * (src/fortran_src/wrap.f90:657-690) for `nmodels` independent models.
+ *   params     [nmodels]
+ *   start      [nmodels*nspec] initial abundances or NULL (elemental start)
+ *   max_rows   rows available per model (TIMEPOINTS+1 in the reference)
+ *   phys_out   [nmodels*max_rows*UCL_N_PHYS] out (row-major per model)
+ *   abund_out  [nmodels*max_rows*nspec] out
+ *   nrows_out  [nmodels] out: rows written
+ *   flag_out   [nmodels] out: 0 or UCL_* per-model error code
+ *   stats_out  [nmodels] out (may be NULL)
+ *   precision  UCL_PREC_FP64 or UCL_PREC_MIXED */
+int ucl_solve_models(ucl_ctx* ctx, int nmodels, const ucl_model_params* params,
+                     const double* start, int max_rows, double* phys_out,
+                     double* abund_out, int* nrows_out, int* flag_out,
+                     ucl_model_stats* stats_out, int precision);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* UCLCHEM_GB300_H */

@@ -1,0 +1,143 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+Used by tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg to
+check and time the GPU path against a CPU restatement of UCLCHEM's rates,
+GETYDOT and DVODE (see ucl_oracle.c).  The product never imports this.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import build as _build
+from uclchem_gb300 import network as _network
+from uclchem_gb300.params import PARAMS_DTYPE, make_param_array, make_params
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_vp = ctypes.c_void_p
+
+
+def _ptr(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+class Oracle:
+    """One loaded network in the oracle."""
+
+    def __init__(self, blob_path: Optional[str] = None):
+        lib = ctypes.CDLL(_build.build())
+        lib.orc_net_load.restype = _vp
+        lib.orc_net_load.argtypes = [ctypes.c_char_p]
+        lib.orc_net_free.argtypes = [_vp]
+        lib.orc_net_set_ions.argtypes = [_vp, ctypes.c_int, _ip]
+        lib.orc_cloud.restype = ctypes.c_int
+        lib.orc_cloud.argtypes = [_vp, _vp, _dp, ctypes.c_int, _dp, _dp, _ip, _i64p]
+        lib.orc_cloud_batch.argtypes = [_vp, ctypes.c_int, _vp, _dp, ctypes.c_int, _dp, _dp, _ip, _ip, _i64p,
+                                        ctypes.c_int]
+        lib.orc_rates.argtypes = [_vp, _vp, _dp, ctypes.c_double, _dp, _dp]
+        lib.orc_rhs.argtypes = [_vp, _vp, _dp, _dp, _dp, _dp]
+        lib.orc_get_odes.argtypes = [_vp, _vp, _dp, _dp]
+        lib.orc_fd_jacobian.argtypes = [_vp, _vp, _dp, _dp, _dp, ctypes.c_double, _dp]
+        lib.orc_photo_rates.argtypes = [_vp, _vp, _dp, _dp]
+        self.lib = lib
+        path = blob_path or _network.DEFAULT_BLOB
+        self.net = lib.orc_net_load(path.encode())
+        if not self.net:
+            raise RuntimeError(f"oracle could not load network {path}")
+        self.tables = _network.Network.load_npz(path.replace(".uclnet", ".npz")) \
+            if path.endswith(".uclnet") else None
+        if self.tables is not None:
+            ions = np.array([i for i, s in enumerate(self.tables.species) if "+" in s], dtype=np.int32)
+            lib.orc_net_set_ions(self.net, len(ions), _ptr(ions, _ip))
+        self.nspec = self.tables.nspec if self.tables is not None else None
+        self.nreac = self.tables.nreac if self.tables is not None else None
+
+    def __del__(self):
+        try:
+            self.lib.orc_net_free(self.net)
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------------ #
+    def cloud(self, param_dict=None, start=None, max_rows: int = 501):
+        """One CLOUD model; returns (phys[rows,8], abund[rows,nspec], flag, counters)."""
+        p = make_params(param_dict)
+        phys = np.zeros((max_rows, 8))
+        ab = np.zeros((max_rows, self.nspec))
+        nrows = ctypes.c_int(0)
+        cnt = np.zeros(9, dtype=np.int64)
+        st = None if start is None else np.ascontiguousarray(start, dtype=np.float64)
+        flag = self.lib.orc_cloud(self.net, p.ctypes.data, None if st is None else _ptr(st), max_rows,
+                                  _ptr(phys), _ptr(ab), ctypes.byref(nrows), _ptr(cnt, _i64p))
+        n = nrows.value
+        return phys[:n], ab[:n], flag, cnt
+
+    def cloud_batch(self, dicts: Sequence[dict], max_rows: int = 501, nthreads: int = 0):
+        params = make_param_array(dicts)
+        m = len(params)
+        phys = np.zeros((m, max_rows, 8))
+        ab = np.zeros((m, max_rows, self.nspec))
+        nrows = np.zeros(m, dtype=np.int32)
+        flags = np.zeros(m, dtype=np.int32)
+        cnt = np.zeros((m, 9), dtype=np.int64)
+        nthreads = nthreads or os.cpu_count() or 1
+        self.lib.orc_cloud_batch(self.net, m, params.ctypes.data, None, max_rows, _ptr(phys), _ptr(ab),
+                                 _ptr(nrows, _ip), _ptr(flags, _ip), _ptr(cnt, _i64p), nthreads)
+        return phys, ab, nrows, flags, cnt
+
+    def rates(self, param_dict, abund, phi=None):
+        """Rates at the start of an interval; abund [neq] (surface/bulk totals refreshed)."""
+        p = make_params(param_dict)
+        ab = np.ascontiguousarray(abund, dtype=np.float64).copy()
+        out = np.zeros(self.nreac)
+        phys = np.zeros(4)
+        phi = float(p["phi"]) if phi is None else float(phi)
+        self.lib.orc_rates(self.net, p.ctypes.data, _ptr(ab), phi, _ptr(out), _ptr(phys))
+        return out, ab, phys
+
+    def rhs(self, param_dict, y, rates):
+        p = make_params(param_dict)
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        r = np.ascontiguousarray(rates, dtype=np.float64)
+        ydot = np.zeros(self.nspec + 1)
+        scale = np.zeros(self.nspec + 1)
+        self.lib.orc_rhs(self.net, p.ctypes.data, _ptr(y), _ptr(r), _ptr(ydot), _ptr(scale))
+        return ydot, scale
+
+    def photo_rates(self, param_dict, y):
+        """(H2, CO) photodissociation rates that F evaluates at state y."""
+        p = make_params(param_dict)
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        out = np.zeros(2)
+        self.lib.orc_photo_rates(self.net, p.ctypes.data, _ptr(y), _ptr(out))
+        return out
+
+    def get_odes(self, param_dict, abund):
+        p = make_params(param_dict)
+        a = np.ascontiguousarray(abund, dtype=np.float64)
+        ydot = np.zeros(self.nspec + 1)
+        flag = self.lib.orc_get_odes(self.net, p.ctypes.data, _ptr(a), _ptr(ydot))
+        return ydot, flag
+
+    def fd_jacobian(self, param_dict, y, rates, ewt_inv, h):
+        p = make_params(param_dict)
+        n = self.nspec + 1
+        jac = np.zeros(n * n)
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        r = np.ascontiguousarray(rates, dtype=np.float64)
+        w = np.ascontiguousarray(ewt_inv, dtype=np.float64)
+        self.lib.orc_fd_jacobian(self.net, p.ctypes.data, _ptr(y), _ptr(r), _ptr(w), float(h), _ptr(jac))
+        return jac.reshape(n, n).T  # row i, column j
+
+
+def initial_abundances(oracle: Oracle, param_dict=None):
+    """Elemental start vector (initializeChemistry) via a zero-length model."""
+    d = dict(param_dict or {})
+    d["finalTime"] = 0.0
+    phys, ab, flag, _ = oracle.cloud(d, max_rows=2)
+    return ab[0], phys[0]
