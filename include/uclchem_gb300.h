@@ -125,9 +125,9 @@ int ucl_rhs_batch(ucl_ctx* ctx, int nsys, const ucl_model_params* params,
                   const double* y, const double* rates, const double* av,
                   double* ydot);
 
-/* Analytic Jacobian dF/dy for `nsys` systems, dense column-major NEQ x NEQ
- * per system (the matrix DVODE's MITER=2 branch approximates by finite
- * differences, dvode.f90:8331-8355).  jac [nsys*NEQ*NEQ] out. */
+/* Analytic Jacobian dF/dy for `nsys` systems, dense row-major NEQ x NEQ per
+ * system: jac[s*NEQ*NEQ + i*NEQ + j] = dF_i/dy_j (the matrix DVODE's MITER=2
+ * branch approximates by finite differences, dvode.f90:8331-8355). */
 int ucl_jac_batch(ucl_ctx* ctx, int nsys, const ucl_model_params* params,
                   const double* y, const double* rates, const double* av,
                   double* jac);
@@ -145,7 +145,8 @@ typedef struct ucl_model_stats {
  * (io.f90:74-82).  Replaces the time loop of solveAbundances
  * (src/fortran_src/wrap.f90:657-690) for `nmodels` independent models.
  *   params     [nmodels]
- *   start      [nmodels*nspec] initial abundances or NULL (elemental start)
+ *   start      [nmodels*NEQ] initial abundances + density, or NULL
+ *              (elemental start of initializeChemistry)
  *   max_rows   rows available per model (TIMEPOINTS+1 in the reference)
  *   phys_out   [nmodels*max_rows*UCL_N_PHYS] out (row-major per model)
  *   abund_out  [nmodels*max_rows*nspec] out
@@ -157,6 +158,20 @@ int ucl_solve_models(ucl_ctx* ctx, int nmodels, const ucl_model_params* params,
                      const double* start, int max_rows, double* phys_out,
                      double* abund_out, int* nrows_out, int* flag_out,
                      ucl_model_stats* stats_out, int precision);
+
+/* Same as ucl_solve_models with every array already in device memory of the
+ * context's GPU (no host copies; the call only enqueues work).  `stream` is a
+ * cudaStream_t (NULL = the context's stream); `max_ctas` caps the number of
+ * concurrently integrated models (0 = as many as fit).  Completion is
+ * observed by synchronising that stream. */
+int ucl_solve_models_device(ucl_ctx* ctx, int nmodels, const ucl_model_params* params_dev,
+                            const double* start_dev, int max_rows, double* phys_dev,
+                            double* abund_dev, int* nrows_dev, int* flag_dev,
+                            ucl_model_stats* stats_dev, int precision, int max_ctas,
+                            void* stream);
+
+/* Models the context integrates concurrently at the given precision. */
+int ucl_ctx_slots(const ucl_ctx* ctx, int precision);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,73 @@
+"""Whole-model parity on the GPU: CLOUD models through ucl_solve_models (the
+C ABI) against the oracle, the reference's golden output and conservation."""
+import numpy as np
+import pytest
+
+from conftest import dex_error
+from uclchem_gb300.analysis import element_counts
+from uclchem_gb300.params import grid_params, make_param_array
+
+pytestmark = pytest.mark.gpu
+
+CONFIG1 = {"initialDens": 1e4, "initialTemp": 10.0, "finalTime": 1e6}
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from uclchem_gb300 import _lib, network
+    c = _lib.Context(network.DEFAULT_BLOB, device=0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def config1_oracle(oracle):
+    return oracle.cloud(CONFIG1, max_rows=64)
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_config1_matches_oracle_and_golden(ctx, oracle, config1_oracle, static_golden, precision):
+    params = make_param_array([CONFIG1])
+    phys, ab, nrows, flags, stats = ctx.solve_models(params, 64, precision=precision)
+    ophys, oab, oflag, _ = config1_oracle
+    n = int(nrows[0])
+    assert flags[0] == 0 and n == len(ophys) == 47
+    np.testing.assert_allclose(phys[0, :n, 0], ophys[:, 0], rtol=1e-12)
+    np.testing.assert_allclose(phys[0, :n, 1:7], ophys[:, 1:7], rtol=1e-12)
+    assert dex_error(ab[0, :n], oab) < 0.01
+    assert dex_error(ab[0, :n], static_golden["abund"]) < 0.01
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_grid_points_match_oracle(ctx, oracle, precision):
+    dicts = grid_params(6, seed=20261203, final_time=1e5)
+    params = make_param_array(dicts)
+    phys, ab, nrows, flags, stats = ctx.solve_models(params, 64, precision=precision)
+    ophys, oab, onrows, oflags, _ = oracle.cloud_batch(dicts, max_rows=64)
+    for k in range(len(dicts)):
+        assert flags[k] == oflags[k] == 0
+        assert nrows[k] == onrows[k]
+        n = int(nrows[k])
+        assert dex_error(ab[k, :n], oab[k, :n]) < 0.01, k
+
+
+def test_element_conservation(ctx, net):
+    params = make_param_array([CONFIG1])
+    for precision in (0, 1):
+        phys, ab, nrows, flags, stats = ctx.solve_models(params, 64, precision=precision)
+        n = int(nrows[0])
+        for e in ["H", "C", "N", "O", "S", "HE"]:
+            tot = ab[0, :n] @ element_counts(net.species, e)
+            assert np.abs(tot / tot[0] - 1).max() < 1e-8, (precision, e)
+
+
+def test_failure_codes_from_host_injection(ctx):
+    """MXSTEP=1 makes every DVODE call return ISTATE=-1; the retry loop then
+    ends the model with INT_TOO_MANY_FAILS_ERROR, exactly as the oracle."""
+    params = make_param_array([{"initialDens": 1e4, "finalTime": 1e3}])
+    params[0]["mxstep"] = 1
+    phys, ab, nrows, flags, stats = ctx.solve_models(params, 64, precision=1)
+    assert flags[0] == -5
+    params = make_param_array([CONFIG1])
+    phys, ab, nrows, flags, stats = ctx.solve_models(params, 8, precision=1)
+    assert flags[0] == -6 and nrows[0] == 8

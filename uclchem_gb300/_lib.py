@@ -1,0 +1,172 @@
+"""ctypes binding of the C ABI (include/uclchem_gb300.h).
+
+The library is built in-tree (uclchem_gb300/build.py).  There is no CPU
+fallback: every entry point raises if the CUDA library cannot be loaded or
+returns an error code.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import build as _build
+from .params import ModelParams
+
+_vp = ctypes.c_void_p
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+class ModelStats(ctypes.Structure):
+    _fields_ = [("nst", ctypes.c_int64), ("nfe", ctypes.c_int64), ("nje", ctypes.c_int64),
+                ("nlu", ctypes.c_int64), ("nni", ctypes.c_int64), ("ncfn", ctypes.c_int64),
+                ("netf", ctypes.c_int64), ("n_intervals", ctypes.c_int32), ("n_retries", ctypes.c_int32),
+                ("solve_ms", ctypes.c_double)]
+
+
+STATS_DTYPE = np.dtype([(n, np.int64) for n in ("nst", "nfe", "nje", "nlu", "nni", "ncfn", "netf")] +
+                       [("n_intervals", np.int32), ("n_retries", np.int32), ("solve_ms", np.float64)])
+assert STATS_DTYPE.itemsize == ctypes.sizeof(ModelStats)
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+EXPORTS = ["ucl_params_default", "ucl_network_load", "ucl_network_free", "ucl_network_nspec",
+           "ucl_network_nreac", "ucl_ctx_create", "ucl_ctx_destroy", "ucl_rates_batch", "ucl_rhs_batch",
+           "ucl_jac_batch", "ucl_solve_models", "ucl_solve_models_device", "ucl_ctx_slots"]
+
+_LOCK = threading.Lock()
+_LIB = None
+
+
+class UclError(RuntimeError):
+    pass
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load libuclchem_gb300.so (building it in-tree if needed)."""
+    global _LIB
+    with _LOCK:
+        if _LIB is not None:
+            return _LIB
+        path = _build.LIB
+        if build_if_missing and (not os.path.exists(path) or _build.needs_build()):
+            _build.build()
+        if not os.path.exists(path):
+            raise UclError("CUDA library not built: run uclchem_gb300.build.build()")
+        lib = ctypes.CDLL(path)
+        lib.ucl_params_default.argtypes = [ctypes.POINTER(ModelParams)]
+        lib.ucl_network_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(_vp)]
+        lib.ucl_network_free.argtypes = [_vp]
+        lib.ucl_network_nspec.argtypes = [_vp]
+        lib.ucl_network_nreac.argtypes = [_vp]
+        lib.ucl_ctx_create.argtypes = [_vp, ctypes.c_int, ctypes.c_size_t, ctypes.POINTER(_vp)]
+        lib.ucl_ctx_destroy.argtypes = [_vp]
+        lib.ucl_rates_batch.argtypes = [_vp, ctypes.c_int, _vp, _dp, _dp, _dp, _dp]
+        lib.ucl_rhs_batch.argtypes = [_vp, ctypes.c_int, _vp, _dp, _dp, _dp, _dp]
+        lib.ucl_jac_batch.argtypes = [_vp, ctypes.c_int, _vp, _dp, _dp, _dp, _dp]
+        lib.ucl_solve_models.argtypes = [_vp, ctypes.c_int, _vp, _dp, ctypes.c_int, _dp, _dp, _ip, _ip, _vp,
+                                         ctypes.c_int]
+        lib.ucl_solve_models_device.argtypes = [_vp, ctypes.c_int, _vp, _vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp,
+                                                ctypes.c_int, ctypes.c_int, _vp]
+        lib.ucl_ctx_slots.argtypes = [_vp, ctypes.c_int]
+        _LIB = lib
+        return lib
+
+
+def check(rc: int, what: str) -> None:
+    if rc != 0:
+        raise UclError(f"{what} failed with code {rc}")
+
+
+def _p(a):
+    return a.ctypes.data_as(_dp)
+
+
+class Context:
+    """A loaded network on one GPU (ucl_ctx)."""
+
+    def __init__(self, blob_path: str, device: int = 0, hbm_budget: int = 0):
+        lib = load()
+        self.lib = lib
+        net = _vp()
+        check(lib.ucl_network_load(blob_path.encode(), ctypes.byref(net)), "ucl_network_load")
+        self.net = net
+        self.nspec = lib.ucl_network_nspec(net)
+        self.nreac = lib.ucl_network_nreac(net)
+        self.neq = self.nspec + 1
+        ctx = _vp()
+        check(lib.ucl_ctx_create(net, device, hbm_budget, ctypes.byref(ctx)), "ucl_ctx_create")
+        self.ctx = ctx
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.ucl_ctx_destroy(self.ctx)
+            self.ctx = None
+        if getattr(self, "net", None):
+            self.lib.ucl_network_free(self.net)
+            self.net = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def slots(self, precision: int) -> int:
+        return self.lib.ucl_ctx_slots(self.ctx, precision)
+
+    # ---------------------------------------------------------------- #
+    def rates(self, params: np.ndarray, abund: np.ndarray, av: np.ndarray, phi: np.ndarray):
+        n = len(params)
+        ab = np.ascontiguousarray(abund, dtype=np.float64).reshape(n, self.neq).copy()
+        av = np.ascontiguousarray(av, dtype=np.float64)
+        ph = np.ascontiguousarray(phi, dtype=np.float64).copy()
+        out = np.zeros((n, self.nreac))
+        check(self.lib.ucl_rates_batch(self.ctx, n, params.ctypes.data, _p(ab), _p(av), _p(ph), _p(out)),
+              "ucl_rates_batch")
+        return out, ab, ph
+
+    def rhs(self, params, y, rates, av):
+        n = len(params)
+        y = np.ascontiguousarray(y, dtype=np.float64).reshape(n, self.neq)
+        r = np.ascontiguousarray(rates, dtype=np.float64).reshape(n, self.nreac)
+        av = np.ascontiguousarray(av, dtype=np.float64)
+        out = np.zeros((n, self.neq))
+        check(self.lib.ucl_rhs_batch(self.ctx, n, params.ctypes.data, _p(y), _p(r), _p(av), _p(out)),
+              "ucl_rhs_batch")
+        return out
+
+    def jac(self, params, y, rates, av):
+        n = len(params)
+        y = np.ascontiguousarray(y, dtype=np.float64).reshape(n, self.neq)
+        r = np.ascontiguousarray(rates, dtype=np.float64).reshape(n, self.nreac)
+        av = np.ascontiguousarray(av, dtype=np.float64)
+        out = np.zeros((n, self.neq, self.neq))
+        check(self.lib.ucl_jac_batch(self.ctx, n, params.ctypes.data, _p(y), _p(r), _p(av), _p(out)),
+              "ucl_jac_batch")
+        return out
+
+    def solve_models(self, params: np.ndarray, max_rows: int, start=None, precision: int = PREC_MIXED):
+        n = len(params)
+        phys = np.zeros((n, max_rows, 8))
+        ab = np.zeros((n, max_rows, self.nspec))
+        nrows = np.zeros(n, dtype=np.int32)
+        flags = np.zeros(n, dtype=np.int32)
+        stats = np.zeros(n, dtype=STATS_DTYPE)
+        st = None
+        if start is not None:
+            st = np.ascontiguousarray(start, dtype=np.float64).reshape(n, self.neq)
+        check(self.lib.ucl_solve_models(self.ctx, n, params.ctypes.data, None if st is None else _p(st), max_rows,
+                                        _p(phys), _p(ab), nrows.ctypes.data_as(_ip), flags.ctypes.data_as(_ip),
+                                        stats.ctypes.data, precision), "ucl_solve_models")
+        return phys, ab, nrows, flags, stats
+
+    def solve_models_device(self, n, params_ptr, start_ptr, max_rows, phys_ptr, abund_ptr, nrows_ptr, flags_ptr,
+                            stats_ptr, precision, max_ctas=0, stream=0):
+        check(self.lib.ucl_solve_models_device(self.ctx, n, params_ptr, start_ptr, max_rows, phys_ptr, abund_ptr,
+                                               nrows_ptr, flags_ptr, stats_ptr, precision, max_ctas, stream),
+              "ucl_solve_models_device")

@@ -1,0 +1,151 @@
+// Shared definitions of the GB300 chemistry solver: device table layout,
+// physical constants and block-level helpers.
+//
+// The device tables are compiled on the host (ucl_capi.cu) from the MakeRates
+// network (network.f90 + odes.f90 via uclchem_gb300/network.py) into
+//  * per-reaction rate recipes (type code + precomputed constants) that follow
+//    the block structure of calculateReactionRates (src/fortran_src/rates.f90:21-343);
+//  * the flux form of GETYDOT (odes.f90): one flux per reaction and a
+//    signed species-row CSR, split into balanced chunks;
+//  * the analytic Jacobian's structural entries.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ucl {
+
+constexpr int NT = 256;          // threads per CTA of the solver kernels
+constexpr int NWARP = NT / 32;
+constexpr int MAX_NEQ = 520;     // largest NEQ the kernels are compiled for
+constexpr int LMAXP = 7;         // Nordsieck columns held (MAXORD+2)
+
+// Reaction types (the block of calculateReactionRates that last writes the
+// reaction's rate; rates.f90:33-342).
+enum RType : uint8_t {
+  RT_NONE = 0, RT_CRP, RT_PHOTON, RT_CRPHOT, RT_FREEZE, RT_DESOH2, RT_DESCR, RT_DEUVCR,
+  RT_CRS, RT_EXRELAX, RT_EXSOLID, RT_THERM, RT_LH, RT_LHDES, RT_ER, RT_ERDES, RT_H2FORM,
+  RT_ZERO, RT_BULKSWAP, RT_SURFSWAP, RT_TWOBODY, RT_IONOPOL1, RT_IONOPOL2, RT_GAR,
+  RT_EFREEZE,
+};
+
+// Term shapes of the generated RHS (uclchem_gb300/network.py SHAPES).
+enum Shape : uint8_t {
+  SH_DYY = 0, SH_Y, SH_DY, SH_Y_SM, SH_YY, SH_YY_BLR, SH_Y_BLR, SH_DY_SM_Y, SH_Y_TS_SM, SH_DYY_SM,
+};
+
+struct DevNet {
+  int nspec, neq, nreac, three_phase;
+  int n_surface, n_bulk, n_ice;
+  const int* surface_list;
+  const int* bulk_list;
+  // named species (0-based; absent elements point at the density slot)
+  int nh, nh2, nhe, nc, ncx, nco, nelec, nsurf, nbulk, nmgx, nsix, nsx, nclx, no, nn, nmg, np,
+      nf, nna, nli, npah, nd, n18o, n15n, n13c;
+  // named reactions
+  int rx_h2hv, rx_cohv, rx_chv;
+  // ---- rates ----
+  const uint8_t* rtype;
+  const uint8_t* iceflag;  // PHOTON/CRPHOT: 1 surface, 2 bulk reactant; LHDES/ERDES: 1 bulk reactant
+  const int* re1;
+  const double* alpha;
+  const double* beta;
+  const double* gama;
+  const double* tmin;
+  const double* tmax;
+  const uint8_t* extrap;
+  const double* mass_re1;  // FREEZE/ER: mass of the reactant
+  const double* c0;        // per-type constants (see ucl_capi.cu build_tables)
+  const double* c1;
+  const double* c2;
+  const double* c3;
+  const double* c4;
+  const int* partner;      // LH <-> LHDES, ER <-> ERDES, EFREEZE -> HFREEZE
+  const uint8_t* stick;    // FREEZE: 1 = H2 sticking, 2 = H sticking
+  const double* gar;       // GAR parameters, 7 per reaction (row of the GAR block)
+  int n_fp;
+  const int* fp;           // freeze partners
+  const int* fp_re1;
+  int desoh2_1, descr_1, deuvcr_1, therm_1;  // first reaction of each block, -1 = absent
+  // ---- flux form ----
+  const uint8_t* fshape;
+  const int* fya;
+  const int* fyb;
+  int swap_lo, swap_hi;    // reactions whose fluxes sum to totalSwap (bulk swap)
+  int n_ts;                // surface-swap (shape 8) reactions
+  const int* ts_rx;
+  // chunked species-row CSR of signed stoichiometric coefficients
+  int nchunk;
+  const int* ch_row;
+  const int* ch_beg;
+  const int* ch_end;
+  const int* st_rx;
+  const float* st_coef;
+  // ---- analytic Jacobian ----
+  // structural entries: (row, col) with contributions (reaction<<3 | slot, coef)
+  // slot 0: d/dY_a, 1: d/dY_b, 2: d/dD, 3: d/dSURFACE via safeMantle, 4: d/dBULK via blr
+  int n_jent;
+  const int* je_row;
+  const int* je_col;
+  const int* je_beg;
+  const int* je_end;
+  const int* jc_key;
+  const float* jc_coef;
+  // surface-swap rank-1: rows with A_i = sum_r S_ir k_r ya_r / sm over shape-8 reactions
+  int n_arow;
+  const int* ar_row;
+  const int* ar_beg;
+  const int* ar_end;
+  const int* ar_rx;
+  const float* ar_coef;
+  // photo reactions' species rows (for the d rate / d column-density terms)
+  int n_ph;                // species rows of the H2 and CO photo reactions
+  const int* ph_row;
+  const float* ph_c1;      // stoichiometric coefficient in the H2 photodissociation
+  const float* ph_c2;      // stoichiometric coefficient in the CO photodissociation
+};
+
+// Physical constants (constants.f90:2-19, surfacereactions.f90:11-52).
+// Default-REAL literals of the reference are rounded through float.
+struct Consts {
+  double K_BOLTZ, REDUCED_PLANCK, AMU, PI, PC, SECONDS_PER_YEAR;
+  double GRAIN_RADIUS, THERMAL_VEL, GAS_DUST_DENSITY_RATIO, GRAIN_CROSSSECTION_PER_H,
+      GRAIN_SURFACEAREA_PER_H, SURFACE_SITE_DENSITY, VDIFF_PREFACTOR, NUM_SITES_PER_GRAIN,
+      CHEMICAL_BARRIER_THICKNESS, MAX_GRAIN_TEMP, MIN_SURFACE_ABUND, MIN_ABUND;
+  // spline tables (photoreactions.f90:11-41) and their natural-spline second derivatives
+  double lam[30], xlam[30], xlam_y2[30];
+  double nco_grid[8], nh2_grid[6];
+  double sco[7][6], sco_y2[7][6];
+};
+
+// ---------------------------------------------------------------------------
+// block helpers (all threads of the CTA must call)
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int NTH>
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  v = warp_sum(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int i = 0; i < NTH / 32; ++i) s += red[i];
+    red[NTH / 32] = s;
+  }
+  __syncthreads();
+  return red[NTH / 32];
+}
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+}  // namespace ucl

@@ -1,0 +1,115 @@
+"""Python front end mirroring ``uclchem.model`` for the CLOUD model.
+
+``cloud`` keeps the signature and return layout of the reference's
+``uclchem.model.cloud`` (src/uclchem/model.py:227-316): physics array
+``[rows, points, 8]``, abundance array ``[rows, points, nspec]``, rates,
+``abundanceStart`` and the success flag, with rows trimmed as
+``_array_clean`` does (model.py:158-187).  The solve runs on the GPU through
+the C ABI; there is no CPU path.
+
+``cloud_grid`` is the batched sibling: many parameter dictionaries in one
+device launch, one persistent CTA per model.
+"""
+from __future__ import annotations
+
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import network as _network
+from ._lib import PREC_FP64, PREC_MIXED, Context, UclError
+from .params import make_param_array, make_params
+
+TIMEPOINTS = 500
+N_PHYSICAL_PARAMETERS = 8
+PHYSICAL_PARAMETERS = ["Time", "Density", "gasTemp", "dustTemp", "Av", "radfield", "zeta", "dstep"]
+
+_CTX: Optional[Context] = None
+
+
+def get_context(device: int = 0) -> Context:
+    """The process-wide context for the default network on `device`."""
+    global _CTX
+    if _CTX is None:
+        _CTX = Context(_network.DEFAULT_BLOB, device=device)
+    return _CTX
+
+
+def _precision(p) -> int:
+    if p in (PREC_FP64, PREC_MIXED):
+        return p
+    if isinstance(p, str) and p.lower() in ("fp64", "double", "plain"):
+        return PREC_FP64
+    if isinstance(p, str) and p.lower() in ("mixed", "fp32", "tc"):
+        return PREC_MIXED
+    raise ValueError(f"unknown precision {p!r}")
+
+
+def _start_vectors(ctx: Context, params, starting_chemistry, n: int):
+    if starting_chemistry is None:
+        return None
+    st = np.asarray(starting_chemistry, dtype=np.float64)
+    if st.ndim == 1:
+        st = np.broadcast_to(st, (n, st.shape[0]))
+    out = np.zeros((n, ctx.neq))
+    out[:, :min(st.shape[1], ctx.nspec)] = st[:, :ctx.nspec]
+    # density slot: the value the reference holds there (initial density, or
+    # 1.001x it for freefall, chemistry.f90:105 / cloud.f90:29)
+    for i in range(n):
+        d0 = params[i]["initialDens"]
+        out[i, -1] = d0 * float(np.float32(1.001)) if params[i]["freefall"] else d0
+    return out
+
+
+def cloud_grid(param_dicts: Sequence[Optional[dict]], timepoints: int = TIMEPOINTS,
+               starting_chemistry=None, precision="mixed", context: Optional[Context] = None):
+    """Run many static/freefall CLOUD models in one device launch.
+
+    Returns (physics [n, rows, 8], abundances [n, rows, nspec], nrows [n],
+    flags [n], stats [n]) with rows = timepoints + 1.
+    """
+    ctx = context or get_context()
+    params = make_param_array(param_dicts)
+    start = _start_vectors(ctx, params, starting_chemistry, len(params))
+    return ctx.solve_models(params, timepoints + 1, start=start, precision=_precision(precision))
+
+
+def cloud(param_dict=None, out_species: Optional[List[str]] = None, return_array: bool = False,
+          return_dataframe: bool = False, return_rates: bool = False, starting_chemistry=None,
+          timepoints: int = TIMEPOINTS, precision="mixed"):
+    """Single CLOUD model with the reference's calling convention."""
+    if return_rates:
+        raise UclError("return_rates is not available on the device path")
+    if starting_chemistry is not None and not (return_array or return_dataframe):
+        raise AssertionError("starting_chemistry can only be used with return_array or return_dataframe set to True")
+    pd = dict(param_dict or {})
+    file_keys = [k for k in pd if k.lower().endswith("file")]
+    if file_keys:
+        raise RuntimeError("file output is not part of the device path; offending keys: " + ", ".join(file_keys))
+    ctx = get_context()
+    try:
+        make_params(pd)
+    except ValueError:
+        flag = -1
+        if return_array or return_dataframe:
+            return None, None, None, None, flag
+        return [flag]
+    phys, ab, nrows, flags, _ = cloud_grid([pd], timepoints=timepoints, starting_chemistry=starting_chemistry,
+                                           precision=precision, context=ctx)
+    n = int(nrows[0])
+    flag = int(flags[0])
+    species = _network.load_default().species
+    phys_a = phys[0, :n, None, :]
+    chem_a = ab[0, :n, None, :]
+    abundance_start = ab[0, n - 1, :] if n > 0 else None
+    if return_dataframe:
+        import pandas as pd_  # not a dependency of the device path
+        physics_df = pd_.DataFrame(phys_a[:, 0, :], columns=PHYSICAL_PARAMETERS)
+        chem_df = pd_.DataFrame(chem_a[:, 0, :], columns=species)
+        return physics_df, chem_df, None, abundance_start, flag
+    if return_array:
+        return phys_a, chem_a, None, abundance_start, flag
+    if flag < 0 or not out_species:
+        return [flag]
+    idx = [species.index(s) for s in out_species]
+    return [flag] + [float(ab[0, n - 1, i]) for i in idx]
