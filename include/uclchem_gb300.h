@@ -137,6 +137,7 @@ typedef struct ucl_model_stats {
   int64_t nst, nfe, nje, nlu, nni, ncfn, netf; /* DVODE counters, summed   */
   int32_t n_intervals, n_retries;              /* output rows, retry loops  */
   double solve_ms;                              /* device latency of model  */
+  double t_rates_ms, t_rhs_ms, t_jac_ms, t_lu_ms, t_solve_ms; /* phase split  */
 } ucl_model_stats;
 
 /* Integrate whole CLOUD models on the device, one output row per interval

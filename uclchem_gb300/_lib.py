@@ -24,11 +24,14 @@ class ModelStats(ctypes.Structure):
     _fields_ = [("nst", ctypes.c_int64), ("nfe", ctypes.c_int64), ("nje", ctypes.c_int64),
                 ("nlu", ctypes.c_int64), ("nni", ctypes.c_int64), ("ncfn", ctypes.c_int64),
                 ("netf", ctypes.c_int64), ("n_intervals", ctypes.c_int32), ("n_retries", ctypes.c_int32),
-                ("solve_ms", ctypes.c_double)]
+                ("solve_ms", ctypes.c_double), ("t_rates_ms", ctypes.c_double), ("t_rhs_ms", ctypes.c_double),
+                ("t_jac_ms", ctypes.c_double), ("t_lu_ms", ctypes.c_double), ("t_solve_ms", ctypes.c_double)]
 
 
 STATS_DTYPE = np.dtype([(n, np.int64) for n in ("nst", "nfe", "nje", "nlu", "nni", "ncfn", "netf")] +
-                       [("n_intervals", np.int32), ("n_retries", np.int32), ("solve_ms", np.float64)])
+                       [("n_intervals", np.int32), ("n_retries", np.int32), ("solve_ms", np.float64),
+                        ("t_rates_ms", np.float64), ("t_rhs_ms", np.float64), ("t_jac_ms", np.float64),
+                        ("t_lu_ms", np.float64), ("t_solve_ms", np.float64)])
 assert STATS_DTYPE.itemsize == ctypes.sizeof(ModelStats)
 
 PREC_FP64 = 0

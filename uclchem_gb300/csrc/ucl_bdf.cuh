@@ -35,8 +35,11 @@ struct ModelState {
   double t, target, orig, tyears, abstol_factor, dens, coldens;
   int flag, row, loop, fail_count, retries, model, go;
   long long nst, nfe, nje, nlu, nni, ncfn, netf;
-  unsigned long long t0;
+  unsigned long long t0, tp;
+  unsigned long long tacc[5];  // ns in rates, rhs, jac, lu, solve
 };
+
+enum { PH_RATES = 0, PH_RHS, PH_JAC, PH_LU, PH_SOLVE };
 
 struct Shared {
   DvState d;
@@ -45,17 +48,19 @@ struct Shared {
   RhsScal R;
   ucl_model_params P;
   double red[NWARP + 2];
-  int si[72];
+  int si[LU_SI_INTS];
+  int lperm[MAX_NEQ];
 };
 
 // per-CTA workspace (global memory)
 template <typename T>
 struct Slot {
-  double* yh;    // [LMAXP * n] Nordsieck array, column j at yh + j*n
+  double* yh;    // [LMAXP * n] Nordsieck array, column j at yh + j*n (shared memory)
   double* rate;  // [nreac]
   T* J;          // [n*n] saved Jacobian (row-major; scaled for T=float)
   T* P;          // [n*n] LU factors
   int* perm;     // [n]
+  T* scr;        // [2*NB*n] row-interchange staging
 };
 
 template <typename T>
@@ -63,7 +68,7 @@ struct Ctx {
   const DevNet* N;
   Shared* sh;
   int n;
-  double *y, *savf, *acor, *ewt, *atol, *tmp, *wJ;
+  double *y, *savf, *acor, *ewt, *atol, *tmp, *wJ, *wJi;
   T *xs, *xt;
   double *flux, *part, *dfa, *dfb, *vec, *aux;
   char* lu_smem;
@@ -80,27 +85,38 @@ __device__ __forceinline__ double bnorm(const double* v, const double* w, int n,
   return sqrt(s / n);
 }
 
+__device__ __forceinline__ void ph_begin(ModelState& ms) {
+  if (threadIdx.x == 0) ms.tp = globaltimer_ns();
+}
+__device__ __forceinline__ void ph_end(ModelState& ms, int k) {
+  if (threadIdx.x == 0) ms.tacc[k] += globaltimer_ns() - ms.tp;
+}
+
 // y <- P^-1 y with the current factors
 template <typename T>
 __device__ void lin_solve(Ctx<T>& C, double* y) {
   const int n = C.n;
+  ph_begin(C.sh->ms);
   if constexpr (sizeof(T) == 4) {
     for (int i = threadIdx.x; i < n; i += NT) C.xs[i] = (T)(C.wJ[i] * y[i]);
     __syncthreads();
-    block_lusolve<T>(C.W.P, n, C.W.perm, C.xs, C.xt);
-    for (int i = threadIdx.x; i < n; i += NT) y[i] = (double)C.xs[i] / C.wJ[i];
+    block_lusolve<T>(C.W.P, n, C.W.perm, C.xs, C.xt, (T*)C.lu_smem);
+    for (int i = threadIdx.x; i < n; i += NT) y[i] = (double)C.xs[i] * C.wJi[i];
   } else {
     for (int i = threadIdx.x; i < n; i += NT) C.xs[i] = y[i];
     __syncthreads();
-    block_lusolve<T>(C.W.P, n, C.W.perm, C.xs, C.xt);
+    block_lusolve<T>(C.W.P, n, C.W.perm, C.xs, C.xt, (T*)C.lu_smem);
     for (int i = threadIdx.x; i < n; i += NT) y[i] = C.xs[i];
   }
   __syncthreads();
+  ph_end(C.sh->ms, PH_SOLVE);
 }
 
 template <typename T>
 __device__ __forceinline__ void rhs(Ctx<T>& C, const double* y, double* out, bool jac = false) {
+  ph_begin(C.sh->ms);
   dev_rhs(*C.N, C.sh->P, C.sh->S, y, C.W.rate, out, C.flux, C.part, C.sh->R, jac);
+  ph_end(C.sh->ms, PH_RHS);
 }
 
 // DVJAC (MITER=2 decision logic, analytic J) + P = I - h*rl1*J + LU
@@ -110,26 +126,27 @@ __device__ int dv_jac(Ctx<T>& C) {
   const int tid = threadIdx.x, n = C.n;
   if (d.jok) {
     if (tid == 0) { d.nslj = d.nst; d.jcur = 1; d.nje++; }
-    for (int i = tid; i < n; i += NT) C.wJ[i] = C.ewt[i];
+    for (int i = tid; i < n; i += NT) { C.wJ[i] = C.ewt[i]; C.wJi[i] = 1.0 / C.ewt[i]; }
     __syncthreads();
-    dev_jac<(sizeof(T) == 4), T>(*C.N, C.sh->P, C.sh->S, C.y, C.W.rate, C.wJ, C.W.J, C.flux, C.dfa, C.dfb,
-                                 C.vec, C.sh->R);
+    ph_begin(C.sh->ms);
+    dev_jac<(sizeof(T) == 4), T>(*C.N, C.sh->P, C.sh->S, C.y, C.W.rate, C.wJ, C.wJi, C.W.J, C.flux, C.dfa,
+                                 C.dfb, C.vec, C.sh->R);
+    ph_end(C.sh->ms, PH_JAC);
   } else {
     if (tid == 0) d.jcur = 0;
     __syncthreads();
   }
+  ph_begin(C.sh->ms);
   const T con = (T)(-(d.h * d.rl1));
-  const size_t nn = (size_t)n * n;
-  const T* J = C.W.J;
-  T* P = C.W.P;
-  for (size_t idx = tid; idx < nn; idx += NT) {
-    T v = con * J[idx];
-    if (idx / n == idx % n) v += (T)1;
-    P[idx] = v;
-  }
+  form_newton_matrix<T>(C.W.J, C.W.P, n, con);
   if (tid == 0) d.nlu++;
   __syncthreads();
-  const int info = block_lu<T>(P, n, C.W.perm, C.lu_smem, C.sh->si);
+  // LU with partial pivoting in both precisions.  (An explicit FP32 inverse
+  // makes each solve one GEMV but its residual error grows like cond(P)^2;
+  // on this problem it multiplied Newton convergence failures, so the
+  // factors are kept and applied by triangular solves.)
+  const int info = block_lu<T>(C.W.P, n, C.W.perm, C.lu_smem, C.sh->si, C.W.scr, C.sh->lperm);
+  ph_end(C.sh->ms, PH_LU);
   return info != 0;
 }
 

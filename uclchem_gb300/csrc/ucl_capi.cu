@@ -167,6 +167,28 @@ static Consts make_consts() {
   for (int j = 0; j < 7; j++)
     for (int k = 0; k < 6; k++) K.sco[j][k] = sco[k * 7 + j];
   for (int j = 0; j < 7; j++) natural(K.nh2_grid, K.sco[j], 6, K.sco_y2[j]);
+  // column spline over the 7 N(CO) points: second derivatives are linear in
+  // the values, y2 = M y; M from the same recurrence applied to unit vectors
+  for (int k = 0; k < 7; k++) {
+    double e[7] = {0, 0, 0, 0, 0, 0, 0}, y2[7];
+    e[k] = 1.0;
+    natural(K.nco_grid, e, 7, y2);
+    for (int j = 0; j < 7; j++) K.sco_m[j][k] = y2[j];
+  }
+  K.h2_dw = 1.0 / (1000.0 * 1.0e-8);
+  K.h2_r = 8.0e7 / (1.7724539 * K.h2_dw);
+  K.h2_t = 3.02 * pow(K.h2_r * 1.0e+03, -0.064);
+  {  // tau(1000 A)/tau(V) from the natural spline of the extinction curve
+    int lo = 0, hi = 31;
+    const double x = 1000.0;
+    while (hi - lo != 1) { int m = (hi + lo) / 2; if (x > K.lam[m - 1]) lo = m; else hi = m; }
+    if (lo == 0) { lo = 1; hi = 2; }
+    if (lo == 30) { lo = 29; hi = 30; }
+    const double h = K.lam[hi - 1] - K.lam[lo - 1], a = (K.lam[hi - 1] - x) / h, b = (x - K.lam[lo - 1]) / h;
+    double v = a * K.xlam[lo - 1] + b * K.xlam[hi - 1] +
+               ((a * a * a - a) * K.xlam_y2[lo - 1] + (b * b * b - b) * K.xlam_y2[hi - 1]) * (h * h) / 6.0;
+    K.xl1000 = v < 0.0 ? 0.0 : v;
+  }
   return K;
 }
 
@@ -615,7 +637,8 @@ struct ucl_ctx {
 
 template <typename T>
 static size_t slot_bytes(int n, int nreac) {
-  return (size_t)LMAXP * n * 8 + (size_t)nreac * 8 + 2 * (size_t)n * n * sizeof(T) + (size_t)n * 4 + 4 * 256;
+  return (size_t)nreac * 8 + 2 * (size_t)n * n * sizeof(T) + (size_t)n * 4 +
+         (size_t)2 * LuCfg<T>::NB * n * sizeof(T) + 4 * 256;
 }
 
 template <typename T>
@@ -627,6 +650,14 @@ static int max_slots(ucl_ctx* c) {
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_models<T>, NT, L.total) != cudaSuccess)
     return 0;
+  // make sure the per-thread stack covers the kernel's static local memory
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, k_solve_models<T>) == cudaSuccess) {
+    size_t cur = 0;
+    cudaDeviceGetLimit(&cur, cudaLimitStackSize);
+    const size_t need = (fa.localSizeBytes + 1023) / 1024 * 1024 + 1024;
+    if (cur < need) cudaDeviceSetLimit(cudaLimitStackSize, need);
+  }
   return std::max(1, per_sm) * c->nsm;
 }
 
@@ -690,9 +721,12 @@ static int solve_dev(ucl_ctx* c, int nmodels, const ucl_model_params* params_d, 
   nslots = (int)std::min<size_t>(nslots, std::max<size_t>(1, c->budget / per));
   nslots = std::min(nslots, nmodels);
   if (nslots < 1) return UCL_OK;
-  const size_t yh_b = (size_t)nslots * LMAXP * n * 8, rate_b = (size_t)nslots * c->nreac * 8,
-               j_b = (size_t)nslots * n * n * sizeof(T), perm_b = (size_t)nslots * n * 4;
-  int rc = c->ws.ensure(yh_b + rate_b + 2 * j_b + perm_b + 256);
+  // every region 256-byte aligned (the LU uses 16-byte vector accesses)
+  auto a256 = [](size_t x) { return (x + 255) / 256 * 256; };
+  const size_t yh_b = 256, rate_b = a256((size_t)nslots * c->nreac * 8),
+               j_b = a256((size_t)nslots * n * n * sizeof(T)), perm_b = a256((size_t)nslots * n * 4),
+               scr_b = a256((size_t)nslots * 2 * LuCfg<T>::NB * n * sizeof(T));
+  int rc = c->ws.ensure(yh_b + rate_b + 2 * j_b + perm_b + scr_b + 256);
   if (rc) return rc;
   char* base = (char*)c->ws.p;
   SlotArrays<T> A;
@@ -701,7 +735,8 @@ static int solve_dev(ucl_ctx* c, int nmodels, const ucl_model_params* params_d, 
   A.J = (T*)(base + yh_b + rate_b);
   A.P = (T*)(base + yh_b + rate_b + j_b);
   A.perm = (int*)(base + yh_b + rate_b + 2 * j_b);
-  int* counter = (int*)(base + yh_b + rate_b + 2 * j_b + perm_b);
+  A.scr = (T*)(base + yh_b + rate_b + 2 * j_b + perm_b);
+  int* counter = (int*)(base + yh_b + rate_b + 2 * j_b + perm_b + scr_b);
   if (cudaMemsetAsync(counter, 0, sizeof(int), c->stream) != cudaSuccess) return UCL_E_CUDA;
   const SmemLayout L = smem_layout<T>(n, c->nreac, c->tab.nchunk);
   k_solve_models<T><<<nslots, NT, L.total, c->stream>>>(c->tab.dn, params_d, start_d, nmodels, max_rows, phys_d,

@@ -18,7 +18,12 @@ struct SysPhys {
   double T, Td, av, dens, phi, cs;  // gas/dust T, Av, density(dstep), CR-desorption yield, cloudSize/points
   double sm, sb, blr;               // safeMantle, safeBulk, bulkLayersReciprocal at interval start
   double h2col, cocol, ccol;        // column densities at interval start
+  double avt, rf, scat1000;         // Av/1.086, radfield/1.7, dust scattering at 1000 A
 };
+
+// per-interval constants of the photo rates (Av and radfield are fixed over
+// an output interval)
+
 
 // ---------------------------------------------------------------------------
 // splines and photo rates (scalar, one thread)
@@ -76,20 +81,104 @@ __device__ double scatter_fn(double x1, double av) {
   return s;
 }
 
-__device__ double h2_photo(double nh2, double radfield, double av) {
-  const double dw = 1.0 / (1000.0 * 1.0e-8);  // turbVel / (xl * 1e-8)
-  double taud = 0.5 * nh2 * (double)1.5e-2f * 1.0e-2 / dw;
+__device__ double scatter_tl(double tl) {
+  const double c[6] = {1.0, 2.006, -1.438, 7.364e-01, -5.076e-01, -5.920e-02};
+  const double k1[6] = {7.514e-01, 8.490e-01, 1.013, 1.282, 2.005, 5.832};
+  double s = 0.0;
+  if (tl < 1.0) {
+    double e = k1[0] * tl;
+    if (e < 100.0) s = c[0] * exp(-e);
+  } else {
+    for (int i = 1; i < 6; i++) {
+      double e = k1[i] * tl;
+      if (e < 100.0) s = s + c[i] * exp(-e);
+    }
+  }
+  return s;
+}
+
+__device__ void photo_setup(SysPhys& S, double radfield) {
+  S.avt = S.av / 1.086;
+  S.rf = radfield / (double)1.7f;
+  S.scat1000 = scatter_tl(S.avt * cK.xl1000);
+}
+
+// H2 photodissociation with line self-shielding (photoreactions.f90:46-127)
+__device__ double h2_photo_s(double nh2, const SysPhys& S) {
+  const double taud = 0.5 * nh2 * (double)1.5e-2f * 1.0e-2 / cK.h2_dw;
   double sj;
   if (taud == 0.0) sj = 1.0;
   else if (taud < 2.0) sj = exp(-0.6666667 * taud);
   else if (taud < 10.0) sj = 0.638 * pow(taud, -1.25);
   else if (taud < 100.0) sj = 0.505 * pow(taud, -1.15);
   else sj = 0.344 * pow(taud, -1.0667);
-  double r = 8.0e7 / (1.7724539 * dw);
-  double t = 3.02 * pow(r * 1.0e+03, -0.064);
-  double u = sqrt(taud * r) / t;
-  double sr = r / (t * sqrt(0.78539816 + u * u));
-  return 5.18e-11 * (radfield / (double)1.7f) * scatter_fn(1000.0, av) * (sj + sr);
+  const double r = cK.h2_r, t = cK.h2_t;
+  const double u = sqrt(taud * r) / t;
+  const double sr = r / (t * sqrt(0.78539816 + u * u));
+  return 5.18e-11 * S.rf * S.scat1000 * (sj + sr);
+}
+
+// CO photodissociation (photoreactions.f90:57-72, 251-304), evaluated by a
+// whole warp: the seven row splines of the shielding table run in parallel
+// lanes.  All 32 lanes must call; the result is returned in every lane.
+__device__ double co_photo_w(double nh2, double nco, const SysPhys& S) {
+  const int lane = threadIdx.x & 31;
+  const double lu = log10(fabs(nco) + 1.0), lw = log10(fabs(nh2) + 1.0);
+  double lognco = log10(nco + 1.0), lognh2 = log10(nh2 + 1.0);
+  if (lognco < cK.nco_grid[0]) lognco = cK.nco_grid[0];
+  if (lognh2 < cK.nh2_grid[0]) lognh2 = cK.nh2_grid[0];
+  if (lognco > cK.nco_grid[6]) lognco = cK.nco_grid[6];
+  if (lognh2 > cK.nh2_grid[5]) lognh2 = cK.nh2_grid[5];
+  double yy = 0.0;
+  if (lane < 7) yy = spline_eval(cK.nh2_grid, cK.sco[lane], cK.sco_y2[lane], 6, lognh2);
+  double v[7];
+#pragma unroll
+  for (int j = 0; j < 7; j++) v[j] = __shfl_sync(0xffffffffu, yy, j);
+  double y2 = 0.0;
+  if (lane < 7) {
+#pragma unroll
+    for (int k = 0; k < 7; k++) y2 += cK.sco_m[lane][k] * v[k];
+  }
+  double w2[7];
+#pragma unroll
+  for (int j = 0; j < 7; j++) w2[j] = __shfl_sync(0xffffffffu, y2, j);
+  // evaluate the column spline at log N(CO) (unit grid spacing)
+  int jlo = (int)floor(lognco - cK.nco_grid[0]);
+  if (jlo < 0) jlo = 0;
+  if (jlo > 5) jlo = 5;
+  double ya = v[0], yb = v[1], ya2 = w2[0], yb2 = w2[1];
+#pragma unroll
+  for (int j = 1; j < 6; j++)
+    if (jlo == j) { ya = v[j]; yb = v[j + 1]; ya2 = w2[j]; yb2 = w2[j + 1]; }
+  const double a = (cK.nco_grid[jlo + 1] - lognco), b = (lognco - cK.nco_grid[jlo]);
+  const double val = a * ya + b * yb + ((a * a * a - a) * ya2 + (b * b * b - b) * yb2) / 6.0;
+  const double ssf = exp(val * 2.302585092994045684);
+  double lb = (5675.0 - 200.6 * lw) - (571.6 - 24.09 * lw) * lu + (18.22 - 0.7664 * lw) * (lu * lu);
+  if (lb > 1076.1) lb = 1076.1;
+  if (lb < 913.6) lb = 913.6;
+  const double tl = S.avt * xlambda(lb);
+  // scatter: lanes 1..5 take one exponential each
+  const double c[6] = {1.0, 2.006, -1.438, 7.364e-01, -5.076e-01, -5.920e-02};
+  const double k1[6] = {7.514e-01, 8.490e-01, 1.013, 1.282, 2.005, 5.832};
+  double term = 0.0;
+  if (tl < 1.0) {
+    if (lane == 0) { const double e = k1[0] * tl; if (e < 100.0) term = c[0] * exp(-e); }
+  } else if (lane >= 1 && lane < 6) {
+    const double e = k1[lane] * tl;
+    if (e < 100.0) term = c[lane] * exp(-e);
+  }
+  double sca = 0.0;
+#pragma unroll
+  for (int j = 0; j < 6; j++) sca += __shfl_sync(0xffffffffu, term, j);
+  return (2.e-10) * S.rf * ssf * sca;
+}
+
+// scalar versions used once per interval by calculateReactionRates
+__device__ double h2_photo(double nh2, double radfield, double av) {
+  SysPhys S;
+  S.av = av;
+  photo_setup(S, radfield);
+  return h2_photo_s(nh2, S);
 }
 
 __device__ double co_photo(double nh2, double nco, double radfield, double av) {
@@ -293,7 +382,7 @@ __device__ void dev_rates(const DevNet& N, const ucl_model_params& P, SysPhys& S
 // ---------------------------------------------------------------------------
 // Scalars shared by the RHS and the Jacobian of one evaluation
 struct RhsScal {
-  double D, sm, sb, blr, ts, y335, sc, kh2, kco;
+  double D, sm, sb, ism, isb, blr, ts, y335, sc, kh2, kco;
   double dkh2_dn, dkco_dnh2, dkco_dnco;  // d rate / d column density
   int sm_on, blr_on, neg;
 };
@@ -304,77 +393,84 @@ __device__ __forceinline__ double flux_of(int sh, double k, double D, double ya,
     case SH_DYY: return k * D * ya * yb;
     case SH_Y: return k * ya;
     case SH_DY: return k * D * ya;
-    case SH_Y_SM: return k * ya / R.sm;
+    case SH_Y_SM: return k * ya * R.ism;
     case SH_YY: return k * ya * yb;
     case SH_YY_BLR: return k * ya * yb * R.blr;
     case SH_Y_BLR: return k * ya * R.blr;
-    case SH_DY_SM_Y: return k * D * ya / R.sm * yb;
-    case SH_Y_TS_SM: return k * ya * R.ts / R.sm;
-    default: return k * D * ya * yb / R.sm;
+    case SH_DY_SM_Y: return k * D * ya * R.ism * yb;
+    case SH_Y_TS_SM: return k * ya * R.ts * R.ism;
+    default: return k * D * ya * yb * R.ism;
   }
-}
-
-__device__ __forceinline__ void rhs_scalars(const DevNet& N, const double* y, RhsScal& R) {
-  R.D = y[N.neq - 1];
-  R.sm = fmax(1e-30, y[N.nsurf]);
-  R.sb = fmax(1e-30, y[N.nbulk]);
-  const double q = cK.NUM_SITES_PER_GRAIN / (cK.GAS_DUST_DENSITY_RATIO * R.sb);
-  R.blr = q < 1.0 ? q : 1.0;
-  R.sm_on = y[N.nsurf] > 1e-30;
-  R.blr_on = (q < 1.0) && (y[N.nbulk] > 1e-30);
 }
 
 // Right-hand side F(y) of one system.  All threads.  y, ydot, flux, part in
 // shared memory; rate [nreac] anywhere.  With jac_scalars the photo-rate
 // derivatives needed by the Jacobian are also formed.
+//   warp 0: CO photodissociation (lane-parallel shielding splines)
+//   warp 1: H2 photodissociation
+//   warps 2..: the other reaction fluxes
 __device__ void dev_rhs(const DevNet& N, const ucl_model_params& P, const SysPhys& S, const double* y,
                         const double* rate, double* ydot, double* flux, double* part, RhsScal& R,
                         bool jac_scalars = false) {
-  const int tid = threadIdx.x;
-  const double D = y[N.neq - 1];
-  const double smv = fmax(1e-30, y[N.nsurf]);
-  const double sbv = fmax(1e-30, y[N.nbulk]);
-  const double qv = cK.NUM_SITES_PER_GRAIN / (cK.GAS_DUST_DENSITY_RATIO * sbv);
-  RhsScal L;
-  L.D = D; L.sm = smv; L.sb = sbv; L.blr = qv < 1.0 ? qv : 1.0; L.ts = 0.0;
-  if (tid < 32) {
-    if (tid == 0) {
-      rhs_scalars(N, y, R);
-      const double h2col = 0.5 * y[N.nh2] * D * S.cs;
-      const double cocol = 0.5 * y[N.nco] * D * S.cs;
-      R.kh2 = h2_photo(h2col, P.radfield, S.av);
-      R.kco = co_photo(h2col, cocol, P.radfield, S.av);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    R.D = y[N.neq - 1];
+    R.sm = fmax(1e-30, y[N.nsurf]);
+    R.sb = fmax(1e-30, y[N.nbulk]);
+    R.ism = 1.0 / R.sm;
+    R.isb = 1.0 / R.sb;
+    const double q = cK.NUM_SITES_PER_GRAIN / (cK.GAS_DUST_DENSITY_RATIO * R.sb);
+    R.blr = q < 1.0 ? q : 1.0;
+    R.sm_on = y[N.nsurf] > 1e-30;
+    R.blr_on = (q < 1.0) && (y[N.nbulk] > 1e-30);
+    R.ts = 0.0;
+  }
+  __syncthreads();
+  const double D = R.D;
+  const double h2col = 0.5 * y[N.nh2] * D * S.cs;
+  if (warp == 0) {
+    const double cocol = 0.5 * y[N.nco] * D * S.cs;
+    const double k = co_photo_w(h2col, cocol, S);
+    double d1 = 0.0, d2 = 0.0;
+    if (jac_scalars) {
+      const double e = 1e-6;
+      const double dh = h2col * e + 1e-30, dc = cocol * e + 1e-30;
+      d1 = (co_photo_w(h2col + dh, cocol, S) - k) / dh;
+      d2 = (co_photo_w(h2col, cocol + dc, S) - k) / dc;
+    }
+    if (lane == 0) { R.kco = k; R.dkco_dnh2 = d1; R.dkco_dnco = d2; }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      R.kh2 = h2_photo_s(h2col, S);
       if (jac_scalars) {
-        const double e = 1e-6;
-        const double dh = h2col * e + 1e-30, dc = cocol * e + 1e-30;
-        R.dkh2_dn = (h2_photo(h2col + dh, P.radfield, S.av) - R.kh2) / dh;
-        R.dkco_dnh2 = (co_photo(h2col + dh, cocol, P.radfield, S.av) - R.kco) / dh;
-        R.dkco_dnco = (co_photo(h2col, cocol + dc, P.radfield, S.av) - R.kco) / dc;
+        const double dh = h2col * 1e-6 + 1e-30;
+        R.dkh2_dn = (h2_photo_s(h2col + dh, S) - R.kh2) / dh;
       }
     }
   } else {
-    for (int r = tid - 32; r < N.nreac; r += NT - 32) {
+    for (int r = tid - 64; r < N.nreac; r += NT - 64) {
       const int sh = N.fshape[r];
       if (sh == SH_Y_TS_SM) continue;
       const int b = N.fyb[r];
-      flux[r] = flux_of(sh, rate[r], D, y[N.fya[r]], b >= 0 ? y[b] : 0.0, L);
+      flux[r] = flux_of(sh, rate[r], D, y[N.fya[r]], b >= 0 ? y[b] : 0.0, R);
     }
   }
   __syncthreads();
   // photo fluxes, totalSwap and the surface-swap fluxes (warp 0)
-  if (tid < 32) {
-    if (tid == 0) {
+  if (warp == 0) {
+    if (lane == 0) {
       flux[N.rx_h2hv] = flux_of(N.fshape[N.rx_h2hv], R.kh2, D, y[N.fya[N.rx_h2hv]],
-                                N.fyb[N.rx_h2hv] >= 0 ? y[N.fyb[N.rx_h2hv]] : 0.0, L);
+                                N.fyb[N.rx_h2hv] >= 0 ? y[N.fyb[N.rx_h2hv]] : 0.0, R);
       flux[N.rx_cohv] = flux_of(N.fshape[N.rx_cohv], R.kco, D, y[N.fya[N.rx_cohv]],
-                                N.fyb[N.rx_cohv] >= 0 ? y[N.fyb[N.rx_cohv]] : 0.0, L);
+                                N.fyb[N.rx_cohv] >= 0 ? y[N.fyb[N.rx_cohv]] : 0.0, R);
     }
     double s = 0.0;
-    for (int r = N.swap_lo + tid; r < N.swap_hi; r += 32) s += flux[r];
+    for (int r = N.swap_lo + lane; r < N.swap_hi; r += 32) s += flux[r];
     s = warp_sum(s);
+    RhsScal L = R;
     L.ts = s;
-    if (tid == 0) R.ts = s;
-    for (int k = tid; k < N.n_ts; k += 32) {
+    if (lane == 0) R.ts = s;
+    for (int k = lane; k < N.n_ts; k += 32) {
       const int r = N.ts_rx[k];
       flux[r] = flux_of(SH_Y_TS_SM, rate[r], D, y[N.fya[r]], 0.0, L);
     }
@@ -396,24 +492,25 @@ __device__ void dev_rhs(const DevNet& N, const ucl_model_params& P, const SysPhy
   }
   __syncthreads();
   // surface <-> bulk transfer (odes.f90:4815-5180)
-  if (tid < 32) {
+  if (warp == 0) {
     double s = 0.0;
-    for (int k = tid; k < N.n_surface; k += 32) s += ydot[N.surface_list[k]];
+    for (int k = lane; k < N.n_surface; k += 32) s += ydot[N.surface_list[k]];
     s = warp_sum(s);
     const bool neg = s < 0;
-    const double sc = neg ? fmin(1.0, sbv / smv) : 0.5 * cK.GAS_DUST_DENSITY_RATIO / cK.NUM_SITES_PER_GRAIN;
-    for (int k = tid; k < N.n_surface; k += 32) {
+    const double sc = neg ? fmin(1.0, R.sb * R.ism) : 0.5 * cK.GAS_DUST_DENSITY_RATIO / cK.NUM_SITES_PER_GRAIN;
+    const double f = neg ? s * sc * R.isb : s * sc;
+    for (int k = lane; k < N.n_surface; k += 32) {
       const int si = N.surface_list[k], bi = N.bulk_list[k];
-      const double t = neg ? s * sc * y[bi] / sbv : s * sc * y[si];
+      const double t = f * (neg ? y[bi] : y[si]);
       ydot[si] = ydot[si] - t;
       ydot[bi] = ydot[bi] + t;
     }
     __syncwarp();
     double ss = 0.0, sb = 0.0;
-    for (int k = tid; k < N.n_surface; k += 32) { ss += ydot[N.surface_list[k]]; sb += ydot[N.bulk_list[k]]; }
+    for (int k = lane; k < N.n_surface; k += 32) { ss += ydot[N.surface_list[k]]; sb += ydot[N.bulk_list[k]]; }
     ss = warp_sum(ss);
     sb = warp_sum(sb);
-    if (tid == 0) {
+    if (lane == 0) {
       ydot[N.nsurf] = ss;
       ydot[N.nbulk] = sb;
       ydot[N.neq - 1] = densdot_fn(P, D);
@@ -433,12 +530,12 @@ __device__ void dev_rhs(const DevNet& N, const ucl_model_params& P, const SysPhy
 // on the same y (uses R, flux).  dfa/dfb: [nreac] shared scratch.
 template <bool SCALED, typename T>
 __device__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhys& S, const double* y,
-                        const double* rate, const double* w, T* J, const double* flux, double* dfa, double* dfb,
-                        double* vec, const RhsScal& R) {
+                        const double* rate, const double* w, const double* wi, T* J, const double* flux,
+                        double* dfa, double* dfb, double* vec, const RhsScal& R) {
   const int tid = threadIdx.x;
   const int n = N.neq;
   const size_t nn = (size_t)n * n;
-  const double D = R.D, sm = R.sm;
+  const double D = R.D, ism = R.ism;
   for (size_t i = tid; i < nn; i += NT) J[i] = (T)0;
   for (int r = tid; r < N.nreac; r += NT) {
     const int sh = N.fshape[r];
@@ -450,21 +547,21 @@ __device__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhy
       case SH_DYY: a = k * D * yb; b = k * D * ya; break;
       case SH_Y: a = k; break;
       case SH_DY: a = k * D; break;
-      case SH_Y_SM: a = k / sm; break;
+      case SH_Y_SM: a = k * ism; break;
       case SH_YY: a = k * yb; b = k * ya; break;
       case SH_YY_BLR: a = k * yb * R.blr; b = k * ya * R.blr; break;
       case SH_Y_BLR: a = k * R.blr; break;
-      case SH_DY_SM_Y: a = k * D / sm * yb; b = k * D * ya / sm; break;
-      case SH_Y_TS_SM: a = k * R.ts / sm; break;
-      default: a = k * D * yb / sm; b = k * D * ya / sm; break;
+      case SH_DY_SM_Y: a = k * D * ism * yb; b = k * D * ya * ism; break;
+      case SH_Y_TS_SM: a = k * R.ts * ism; break;
+      default: a = k * D * yb * ism; b = k * D * ya * ism; break;
     }
     dfa[r] = a;
     dfb[r] = b;
   }
   __syncthreads();
   const double invD = 1.0 / D;
-  const double dsm = R.sm_on ? -1.0 / sm : 0.0;
-  const double dblr = R.blr_on ? -1.0 / y[N.nbulk] : 0.0;
+  const double dsm = R.sm_on ? -ism : 0.0;
+  const double dblr = R.blr_on ? -R.isb : 0.0;
   for (int e = tid; e < N.n_jent; e += NT) {
     double v = 0.0;
     for (int c = N.je_beg[e]; c < N.je_end[e]; ++c) {
@@ -481,7 +578,7 @@ __device__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhy
       v += (double)N.jc_coef[c] * d;
     }
     const int i = N.je_row[e], j = N.je_col[e];
-    if (SCALED) J[(size_t)(i) * n + j] = (T)(v * w[i] / w[j]);
+    if (SCALED) J[(size_t)(i) * n + j] = (T)(v * w[i] * wi[j]);
     else J[(size_t)(i) * n + j] = (T)v;
   }
   __syncthreads();
@@ -491,7 +588,7 @@ __device__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhy
     double s = 0.0;
     for (int c = N.ar_beg[a]; c < N.ar_end[a]; ++c) {
       const int r = N.ar_rx[c];
-      s += (double)N.ar_coef[c] * rate[r] * y[N.fya[r]] / sm;
+      s += (double)N.ar_coef[c] * rate[r] * y[N.fya[r]] * ism;
     }
     A[a] = s;
   }
@@ -502,7 +599,7 @@ __device__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhy
     const int r = N.swap_lo + kk;
     const int i = N.ar_row[a], j = N.fya[r];
     const double v = A[a] * rate[r] * R.blr;
-    if (SCALED) J[(size_t)(i) * n + j] += (T)(v * w[i] / w[j]);
+    if (SCALED) J[(size_t)(i) * n + j] += (T)(v * w[i] * wi[j]);
     else J[(size_t)(i) * n + j] += (T)v;
   }
   __syncthreads();
@@ -518,9 +615,9 @@ __device__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhy
     const double dD = (c1 * y1 * R.dkh2_dn + c2 * y2 * R.dkco_dnh2) * half * y[N.nh2] +
                       c2 * y2 * R.dkco_dnco * half * y[N.nco];
     if (SCALED) {
-      J[(size_t)i * n + N.nh2] += (T)(dnh2 * w[i] / w[N.nh2]);
-      J[(size_t)i * n + N.nco] += (T)(dnco * w[i] / w[N.nco]);
-      J[(size_t)i * n + (n - 1)] += (T)(dD * w[i] / w[n - 1]);
+      J[(size_t)i * n + N.nh2] += (T)(dnh2 * w[i] * wi[N.nh2]);
+      J[(size_t)i * n + N.nco] += (T)(dnco * w[i] * wi[N.nco]);
+      J[(size_t)i * n + (n - 1)] += (T)(dD * w[i] * wi[n - 1]);
     } else {
       J[(size_t)i * n + N.nh2] += (T)dnh2;
       J[(size_t)i * n + N.nco] += (T)dnco;
@@ -537,15 +634,14 @@ __device__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhy
   const double y335 = R.y335;
   double* ck = vec;  // [ns] transfer coefficients c_k
   for (int k = tid; k < ns; k += NT)
-    ck[k] = R.neg ? R.sc * y[N.bulk_list[k]] / R.sb : R.sc * y[N.surface_list[k]];
+    ck[k] = R.neg ? R.sc * y[N.bulk_list[k]] * R.isb : R.sc * y[N.surface_list[k]];
   __syncthreads();
   // ice rows: J[s_k,:] -= c_k g ; J[b_k,:] += c_k g  (row-major: threads over columns)
   T* uk = (T*)(vec + 256);  // [2*ns] scaled coefficients
-  const double ws = SCALED ? w[N.nsurf] : 1.0;
   for (int k = tid; k < 2 * ns; k += NT) {
     const int kk = k < ns ? k : k - ns;
     const int row = k < ns ? N.surface_list[kk] : N.bulk_list[kk];
-    const double u = SCALED ? ck[kk] * w[row] / ws : ck[kk];
+    const double u = SCALED ? ck[kk] * w[row] * wi[N.nsurf] : ck[kk];
     uk[k] = (T)(k < ns ? -u : u);
   }
   __syncthreads();
@@ -559,7 +655,7 @@ __device__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhy
   __syncthreads();
   if (tid == 0) {
     // derivative of the coefficients: sparse entries
-    const bool use_sm = R.neg && (R.sb / R.sm < 1.0);
+    const bool use_sm = R.neg && (R.sb * R.ism < 1.0);
     double dsum_col = 0.0;  // sum_k dc_k / d(SURFACE or BULK)
     const int colx = use_sm ? N.nsurf : N.nbulk;
     for (int k = 0; k < ns; ++k) {
@@ -568,8 +664,8 @@ __device__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhy
       int jself;
       if (R.neg) {
         jself = bi;
-        if (use_sm) { dself = 1.0 / R.sm; if (R.sm_on) dx = -y[bi] / (R.sm * R.sm); }
-        else { dself = 1.0 / R.sb; if (y[N.nbulk] > 1e-30) dx = -y[bi] / (R.sb * R.sb); }
+        if (use_sm) { dself = R.ism; if (R.sm_on) dx = -y[bi] * R.ism * R.ism; }
+        else { dself = R.isb; if (y[N.nbulk] > 1e-30) dx = -y[bi] * R.isb * R.isb; }
       } else {
         jself = si;
         dself = R.sc;
@@ -577,10 +673,10 @@ __device__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhy
       dsum_col += dx;
       const double v1 = y335 * dself, v2 = y335 * dx;
       if (SCALED) {
-        J[(size_t)(si) * n + jself] -= (T)(v1 * w[si] / w[jself]);
-        J[(size_t)(bi) * n + jself] += (T)(v1 * w[bi] / w[jself]);
-        J[(size_t)(si) * n + colx] -= (T)(v2 * w[si] / w[colx]);
-        J[(size_t)(bi) * n + colx] += (T)(v2 * w[bi] / w[colx]);
+        J[(size_t)(si) * n + jself] -= (T)(v1 * w[si] * wi[jself]);
+        J[(size_t)(bi) * n + jself] += (T)(v1 * w[bi] * wi[jself]);
+        J[(size_t)(si) * n + colx] -= (T)(v2 * w[si] * wi[colx]);
+        J[(size_t)(bi) * n + colx] += (T)(v2 * w[bi] * wi[colx]);
       } else {
         J[(size_t)(si) * n + jself] -= (T)v1;
         J[(size_t)(bi) * n + jself] += (T)v1;
@@ -595,8 +691,8 @@ __device__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhy
   for (int j = tid; j < n; j += NT) {
     double ssum = 0.0, bsum = 0.0;
     for (int k = 0; k < ns; ++k) {
-      ssum += (double)J[(size_t)N.surface_list[k] * n + j] * (SCALED ? w[N.nsurf] / w[N.surface_list[k]] : 1.0);
-      bsum += (double)J[(size_t)N.bulk_list[k] * n + j] * (SCALED ? w[N.nbulk] / w[N.bulk_list[k]] : 1.0);
+      ssum += (double)J[(size_t)N.surface_list[k] * n + j] * (SCALED ? w[N.nsurf] * wi[N.surface_list[k]] : 1.0);
+      bsum += (double)J[(size_t)N.bulk_list[k] * n + j] * (SCALED ? w[N.nbulk] * wi[N.bulk_list[k]] : 1.0);
     }
     J[(size_t)(N.nsurf) * n + j] = (T)ssum;
     J[(size_t)(N.nbulk) * n + j] = (T)bsum;

@@ -14,7 +14,10 @@
 
 namespace ucl {
 
-constexpr int NT = 256;          // threads per CTA of the solver kernels
+#ifndef UCL_NT
+#define UCL_NT 256
+#endif
+constexpr int NT = UCL_NT;       // threads per CTA of the solver kernels
 constexpr int NWARP = NT / 32;
 constexpr int MAX_NEQ = 520;     // largest NEQ the kernels are compiled for
 constexpr int LMAXP = 7;         // Nordsieck columns held (MAXORD+2)
@@ -115,6 +118,9 @@ struct Consts {
   double lam[30], xlam[30], xlam_y2[30];
   double nco_grid[8], nh2_grid[6];
   double sco[7][6], sco_y2[7][6];
+  double sco_m[7][7];       // natural-spline second derivatives over N(CO) as a linear map
+  double h2_dw, h2_r, h2_t;  // H2 line shielding constants (photoreactions.f90:46-55, 116-123)
+  double xl1000;             // tau(1000 A)/tau(V)
 };
 
 // ---------------------------------------------------------------------------

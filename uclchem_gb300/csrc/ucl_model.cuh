@@ -18,8 +18,10 @@ __device__ double target_time(double ty, double spy) {
   if (ty > 10.0) {
     int k = (int)floor(log10(ty));
     auto p10 = [](int e) { double p = 1.0; for (int i = 0; i < e; ++i) p *= 10.0; return p; };
-    while (p10(k + 1) <= ty) ++k;
-    while (k > 0 && p10(k) > ty) --k;
+    if (k < 1) k = 1;
+    if (k > 5) k = 5;  // 10 < ty < 1e6 here
+    while (k < 5 && p10(k + 1) <= ty) ++k;
+    while (k > 1 && p10(k) > ty) --k;
     const double om = p10(k);
     return ((floor(ty / om) + 1.0) * om) * spy;
   }
@@ -48,6 +50,7 @@ __device__ void interval_start(Ctx<T>& C, bool refresh_density) {
     S.sb = fmax(1e-30, sb);
     const double q = cK.NUM_SITES_PER_GRAIN / (cK.GAS_DUST_DENSITY_RATIO * S.sb);
     S.blr = q < 1.0 ? q : 1.0;
+    photo_setup(S, sh.P.radfield);
   }
   __syncthreads();
 }
@@ -82,7 +85,7 @@ __device__ void run_model(Ctx<T>& C, const ucl_model_params* params, const doubl
   ModelState& ms = sh.ms;
   SysPhys& S = sh.S;
   const DevNet& N = *C.N;
-  const int tid = threadIdx.x, n = C.n, nspec = N.nspec;
+  const int tid = threadIdx.x, n = C.n;
   double* y = C.y;
   if (tid == 0) {
     sh.P = params[mi];
@@ -104,6 +107,7 @@ __device__ void run_model(Ctx<T>& C, const ucl_model_params* params, const doubl
     ms.retries = 0;
     ms.abstol_factor = P.abstol_factor;
     ms.nst = ms.nfe = ms.nje = ms.nlu = ms.nni = ms.ncfn = ms.netf = 0;
+    for (int k = 0; k < 5; k++) ms.tacc[k] = 0;
     sh.d.mxstep = P.mxstep;
     if (P.points != 1 || P.improvedH2CRPDissociation || P.enforceChargeConservation) ms.flag = UCL_PHYSICS_INIT_ERROR;
   }
@@ -159,7 +163,9 @@ __device__ void run_model(Ctx<T>& C, const ucl_model_params* params, const doubl
       __syncthreads();
       if (!ms.go) break;
       interval_start(C, !P.freefall);
+      ph_begin(ms);
       dev_rates(N, P, S, y, C.W.rate, C.aux);
+      ph_end(ms, PH_RATES);
       for (int i = tid; i < n; i += NT) {
         double a = ms.abstol_factor * y[i];
         if (a < P.abstol_min) a = P.abstol_min;
@@ -217,6 +223,11 @@ __device__ void run_model(Ctx<T>& C, const ucl_model_params* params, const doubl
       st.n_intervals = ms.row;
       st.n_retries = ms.retries;
       st.solve_ms = (double)(globaltimer_ns() - ms.t0) * 1e-6;
+      st.t_rates_ms = ms.tacc[PH_RATES] * 1e-6;
+      st.t_rhs_ms = ms.tacc[PH_RHS] * 1e-6;
+      st.t_jac_ms = ms.tacc[PH_JAC] * 1e-6;
+      st.t_lu_ms = ms.tacc[PH_LU] * 1e-6;
+      st.t_solve_ms = ms.tacc[PH_SOLVE] * 1e-6;
       stats[mi] = st;
     }
   }
@@ -226,7 +237,7 @@ __device__ void run_model(Ctx<T>& C, const ucl_model_params* params, const doubl
 // ---------------------------------------------------------------------------
 // shared-memory carve-up of the solver kernels
 struct SmemLayout {
-  size_t y, savf, acor, ewt, atol, tmp, wJ, xs, xt, flux, part, dfa, dfb, vec, aux, lu, total;
+  size_t y, savf, acor, ewt, atol, tmp, wJ, wJi, yh, xs, xt, flux, part, dfa, dfb, vec, aux, lu, total;
 };
 
 template <typename T>
@@ -235,7 +246,8 @@ __host__ __device__ inline SmemLayout smem_layout(int n, int nreac, int nchunk) 
   size_t o = 0;
   auto take = [&](size_t bytes) { size_t r = o; o += (bytes + 15) / 16 * 16; return r; };
   L.y = take(8 * n); L.savf = take(8 * n); L.acor = take(8 * n); L.ewt = take(8 * n);
-  L.atol = take(8 * n); L.tmp = take(8 * n); L.wJ = take(8 * n);
+  L.atol = take(8 * n); L.tmp = take(8 * n); L.wJ = take(8 * n); L.wJi = take(8 * n);
+  L.yh = take(8 * (size_t)LMAXP * n);
   L.xs = take(sizeof(T) * n); L.xt = take(sizeof(T) * n);
   const size_t u0 = o;
   // union: chemistry scratch | rates scratch | LU panel
@@ -259,10 +271,12 @@ __device__ Ctx<T> make_ctx(const DevNet* N, Shared* sh, char* smem, const SmemLa
   C.N = N; C.sh = sh; C.n = N->neq; C.W = W;
   C.y = (double*)(smem + L.y); C.savf = (double*)(smem + L.savf); C.acor = (double*)(smem + L.acor);
   C.ewt = (double*)(smem + L.ewt); C.atol = (double*)(smem + L.atol); C.tmp = (double*)(smem + L.tmp);
-  C.wJ = (double*)(smem + L.wJ); C.xs = (T*)(smem + L.xs); C.xt = (T*)(smem + L.xt);
+  C.wJ = (double*)(smem + L.wJ); C.wJi = (double*)(smem + L.wJi); C.xs = (T*)(smem + L.xs);
+  C.xt = (T*)(smem + L.xt);
   C.flux = (double*)(smem + L.flux); C.part = (double*)(smem + L.part); C.dfa = (double*)(smem + L.dfa);
   C.dfb = (double*)(smem + L.dfb); C.vec = (double*)(smem + L.vec); C.aux = (double*)(smem + L.aux);
   C.lu_smem = smem + L.lu;
+  C.W.yh = (double*)(smem + L.yh);
   return C;
 }
 
@@ -273,22 +287,24 @@ struct SlotArrays {
   T* J;
   T* P;
   int* perm;
+  T* scr;
 };
 
 template <typename T>
 __device__ __forceinline__ Slot<T> slot_of(const SlotArrays<T>& A, int s, int n, int nreac) {
   Slot<T> W;
-  W.yh = A.yh + (size_t)s * LMAXP * n;
+  W.yh = nullptr;  // shared memory, set by make_ctx
   W.rate = A.rate + (size_t)s * nreac;
   W.J = A.J + (size_t)s * n * n;
   W.P = A.P + (size_t)s * n * n;
   W.perm = A.perm + (size_t)s * n;
+  W.scr = A.scr + (size_t)s * 2 * LuCfg<T>::NB * n;
   return W;
 }
 
 // Persistent solver: each CTA pulls model indices from a device counter.
 template <typename T>
-__global__ void __launch_bounds__(NT) k_solve_models(DevNet N, const ucl_model_params* params, const double* start,
+__global__ void __launch_bounds__(NT, 1) k_solve_models(DevNet N, const ucl_model_params* params, const double* start,
                                                      int nmodels, int max_rows, double* phys_out, double* abund_out,
                                                      int* nrows_out, int* flag_out, ucl_model_stats* stats,
                                                      SlotArrays<T> ws, int* counter) {
@@ -344,6 +360,7 @@ __global__ void __launch_bounds__(NT) k_rates(DevNet N, const ucl_model_params* 
     S.sb = fmax(1e-30, sb);
     const double q = cK.NUM_SITES_PER_GRAIN / (cK.GAS_DUST_DENSITY_RATIO * S.sb);
     S.blr = q < 1.0 ? q : 1.0;
+    photo_setup(S, sh.P.radfield);
   }
   __syncthreads();
   dev_rates(N, sh.P, sh.S, y, rates + (size_t)s * N.nreac, aux);
@@ -372,13 +389,15 @@ __global__ void __launch_bounds__(NT) k_rhs_jac(DevNet N, const ucl_model_params
     sh.P = params[s];
     sh.S.av = av[s];
     sh.S.cs = (sh.P.rout - sh.P.rin) * cK.PC / (double)(float)sh.P.points;
+    photo_setup(sh.S, sh.P.radfield);
   }
   __syncthreads();
   const double* r = rates + (size_t)s * N.nreac;
   dev_rhs(N, sh.P, sh.S, y, r, out, flux, part, sh.R, jac != nullptr);
   if (ydot)
     for (int i = threadIdx.x; i < n; i += NT) ydot[(size_t)s * n + i] = out[i];
-  if (jac) dev_jac<false, double>(N, sh.P, sh.S, y, r, nullptr, jac + (size_t)s * n * n, flux, dfa, dfb, vec, sh.R);
+  if (jac)
+    dev_jac<false, double>(N, sh.P, sh.S, y, r, nullptr, nullptr, jac + (size_t)s * n * n, flux, dfa, dfb, vec, sh.R);
 }
 
 }  // namespace ucl
