@@ -171,6 +171,15 @@ int ucl_solve_models_device(ucl_ctx* ctx, int nmodels, const ucl_model_params* p
                             ucl_model_stats* stats_dev, int precision, int max_ctas,
                             void* stream);
 
+/* Batched dense LU with partial pivoting of `nsys` row-major n x n matrices
+ * in device memory (FP32 for UCL_PREC_MIXED, FP64 otherwise), in place: the
+ * factorisation the solver applies to its Newton matrices (the reference's
+ * DGEFA, dvode.f90:11982).  perm_dev[s*n + i] = original row of row i;
+ * info_dev[s] = 0 or the first zero pivot (1-based).  n % 4 == 0 and
+ * mats_dev 16-byte aligned.  `stream` is a cudaStream_t (NULL = context's). */
+int ucl_lu_factor_device(ucl_ctx* ctx, int nsys, int n, int precision, void* mats_dev,
+                         int* perm_dev, int* info_dev, void* stream);
+
 /* Models the context integrates concurrently at the given precision. */
 int ucl_ctx_slots(const ucl_ctx* ctx, int precision);
 

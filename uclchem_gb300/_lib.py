@@ -39,7 +39,8 @@ PREC_MIXED = 1
 
 EXPORTS = ["ucl_params_default", "ucl_network_load", "ucl_network_free", "ucl_network_nspec",
            "ucl_network_nreac", "ucl_ctx_create", "ucl_ctx_destroy", "ucl_rates_batch", "ucl_rhs_batch",
-           "ucl_jac_batch", "ucl_solve_models", "ucl_solve_models_device", "ucl_ctx_slots"]
+           "ucl_jac_batch", "ucl_solve_models", "ucl_solve_models_device", "ucl_ctx_slots",
+           "ucl_lu_factor_device"]
 
 _LOCK = threading.Lock()
 _LIB = None
@@ -76,6 +77,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         lib.ucl_solve_models_device.argtypes = [_vp, ctypes.c_int, _vp, _vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp,
                                                 ctypes.c_int, ctypes.c_int, _vp]
         lib.ucl_ctx_slots.argtypes = [_vp, ctypes.c_int]
+        lib.ucl_lu_factor_device.argtypes = [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp]
         _LIB = lib
         return lib
 
@@ -167,6 +169,10 @@ class Context:
                                         _p(phys), _p(ab), nrows.ctypes.data_as(_ip), flags.ctypes.data_as(_ip),
                                         stats.ctypes.data, precision), "ucl_solve_models")
         return phys, ab, nrows, flags, stats
+
+    def lu_factor_device(self, nsys, n, precision, mats_ptr, perm_ptr, info_ptr, stream=0):
+        check(self.lib.ucl_lu_factor_device(self.ctx, nsys, n, precision, mats_ptr, perm_ptr, info_ptr, stream),
+              "ucl_lu_factor_device")
 
     def solve_models_device(self, n, params_ptr, start_ptr, max_rows, phys_ptr, abund_ptr, nrows_ptr, flags_ptr,
                             stats_ptr, precision, max_ctas=0, stream=0):

@@ -892,6 +892,31 @@ extern "C" int ucl_jac_batch(ucl_ctx* c, int nsys, const ucl_model_params* param
   return rhs_jac(c, nsys, params, y, rates, av, nullptr, jac);
 }
 
+// batched LU of row-major n x n matrices already on the device
+template <typename T>
+static int lu_dev(ucl_ctx* c, int nsys, int n, void* mats, int* perm, int* info, cudaStream_t st) {
+  const size_t scr_b = (size_t)nsys * 2 * LuCfg<T>::NB * n * sizeof(T);
+  int rc = c->small.ensure(scr_b + 256);
+  if (rc) return rc;
+  const size_t sm = lu_smem_bytes<T>(n);
+  if (cudaFuncSetAttribute(k_lu_batch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+    return UCL_E_CUDA;
+  k_lu_batch<T><<<nsys, NT, sm, st>>>((T*)mats, n, perm, info, (T*)c->small.p, nsys);
+  return cuda_status(cudaGetLastError());
+}
+
+extern "C" int ucl_lu_factor_device(ucl_ctx* c, int nsys, int n, int precision, void* mats_dev, int* perm_dev,
+                                    int* info_dev, void* stream) {
+  if (!c || nsys < 0 || n < 2 || n > MAX_NEQ || (n % 4) != 0 || !mats_dev || !perm_dev || !info_dev)
+    return UCL_E_ARG;
+  if (((uintptr_t)mats_dev & 15) != 0) return UCL_E_ARG;
+  if (nsys == 0) return UCL_OK;
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  return precision == UCL_PREC_MIXED ? lu_dev<float>(c, nsys, n, mats_dev, perm_dev, info_dev, st)
+                                     : lu_dev<double>(c, nsys, n, mats_dev, perm_dev, info_dev, st);
+}
+
 // capacity query used by the host front end
 extern "C" int ucl_ctx_slots(const ucl_ctx* c, int precision) {
   if (!c) return 0;

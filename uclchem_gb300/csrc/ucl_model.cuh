@@ -324,6 +324,20 @@ __global__ void __launch_bounds__(NT, 1) k_solve_models(DevNet N, const ucl_mode
   }
 }
 
+// Batched dense LU (ucl_lu_factor_device): one CTA per matrix, the same
+// factorisation the solver applies to its Newton matrices.
+template <typename T>
+__global__ void __launch_bounds__(NT) k_lu_batch(T* mats, int n, int* perm, int* info, T* scr, int nsys) {
+  extern __shared__ __align__(16) char smem[];
+  __shared__ int si[LU_SI_INTS];
+  __shared__ int lperm[MAX_NEQ];
+  const int s = blockIdx.x;
+  if (s >= nsys) return;
+  const int r = block_lu<T>(mats + (size_t)s * n * n, n, perm + (size_t)s * n, smem, si,
+                            scr + (size_t)s * 2 * LuCfg<T>::NB * n, lperm);
+  if (threadIdx.x == 0) info[s] = r;
+}
+
 // Rates for a batch of systems (ucl_rates_batch): one CTA per system.
 __global__ void __launch_bounds__(NT) k_rates(DevNet N, const ucl_model_params* params, double* abund,
                                               const double* av, double* phi, double* rates, int nsys) {
