@@ -182,7 +182,10 @@ def our_arm(args):
     nr_d = torch.empty(M, dtype=torch.int32, device=dev)
     fl_d = torch.empty(M, dtype=torch.int32, device=dev)
     st_d = torch.empty((M, _lib.STATS_DTYPE.itemsize), dtype=torch.uint8, device=dev)
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated stream: the C ABI maps a NULL stream handle (torch's default
+    # stream) to the context's own stream, which the events would not bracket
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
 
     def solve(n, prec):
         ctx.solve_models_device(n, p_d.data_ptr(), None, MAX_ROWS, phys_d.data_ptr(), ab_d.data_ptr(),

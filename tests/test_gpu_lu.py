@@ -18,9 +18,10 @@ def test_batched_lu_reconstructs(precision):
     m = torch.tensor(A, dtype=dt, device="cuda")
     perm = torch.empty((nsys, n), dtype=torch.int32, device="cuda")
     info = torch.empty(nsys, dtype=torch.int32, device="cuda")
-    ctx.lu_factor_device(nsys, n, precision, m.data_ptr(), perm.data_ptr(), info.data_ptr(),
-                         torch.cuda.current_stream().cuda_stream)
-    torch.cuda.synchronize()
+    st = torch.cuda.Stream()
+    st.wait_stream(torch.cuda.current_stream())
+    ctx.lu_factor_device(nsys, n, precision, m.data_ptr(), perm.data_ptr(), info.data_ptr(), st.cuda_stream)
+    st.synchronize()
     LU, p, inf = m.double().cpu().numpy(), perm.cpu().numpy(), info.cpu().numpy()
     assert (inf == 0).all()
     tol = 1e-4 if precision == 1 else 1e-12

@@ -50,6 +50,7 @@ struct Shared {
   double red[NWARP + 2];
   int si[LU_SI_INTS];
   int lperm[MAX_NEQ];
+  TcState tc;
 };
 
 // per-CTA workspace (global memory)
@@ -61,6 +62,7 @@ struct Slot {
   T* P;          // [n*n] LU factors
   int* perm;     // [n]
   T* scr;        // [2*NB*n] row-interchange staging
+  T* dinv;       // [ceil(n/32) * 2 * 1024] inverses of the diagonal blocks of L and U
 };
 
 template <typename T>
@@ -97,18 +99,10 @@ template <typename T>
 __device__ void lin_solve(Ctx<T>& C, double* y) {
   const int n = C.n;
   ph_begin(C.sh->ms);
-  if constexpr (sizeof(T) == 4) {
-    for (int i = threadIdx.x; i < n; i += NT) C.xs[i] = (T)(C.wJ[i] * y[i]);
-    __syncthreads();
-    block_lusolve<T>(C.W.P, n, C.W.perm, C.xs, C.xt, (T*)C.lu_smem);
-    for (int i = threadIdx.x; i < n; i += NT) y[i] = (double)C.xs[i] * C.wJi[i];
-  } else {
-    for (int i = threadIdx.x; i < n; i += NT) C.xs[i] = y[i];
-    __syncthreads();
-    block_lusolve<T>(C.W.P, n, C.W.perm, C.xs, C.xt, (T*)C.lu_smem);
-    for (int i = threadIdx.x; i < n; i += NT) y[i] = C.xs[i];
-  }
-  __syncthreads();
+  if constexpr (sizeof(T) == 4)
+    block_lusolve<T>(C.W.P, n, C.W.perm, C.W.dinv, y, C.wJ, C.wJi, C.xt, (T*)C.lu_smem);
+  else
+    block_lusolve<T>(C.W.P, n, C.W.perm, C.W.dinv, y, nullptr, nullptr, C.xt, (T*)C.lu_smem);
   ph_end(C.sh->ms, PH_SOLVE);
 }
 
@@ -130,7 +124,7 @@ __device__ int dv_jac(Ctx<T>& C) {
     __syncthreads();
     ph_begin(C.sh->ms);
     dev_jac<(sizeof(T) == 4), T>(*C.N, C.sh->P, C.sh->S, C.y, C.W.rate, C.wJ, C.wJi, C.W.J, C.flux, C.dfa,
-                                 C.dfb, C.vec, C.sh->R);
+                                 C.dfb, C.vec, C.part, C.sh->R);
     ph_end(C.sh->ms, PH_JAC);
   } else {
     if (tid == 0) d.jcur = 0;
@@ -145,7 +139,10 @@ __device__ int dv_jac(Ctx<T>& C) {
   // makes each solve one GEMV but its residual error grows like cond(P)^2;
   // on this problem it multiplied Newton convergence failures, so the
   // factors are kept and applied by triangular solves.)
-  const int info = block_lu<T>(C.W.P, n, C.W.perm, C.lu_smem, C.sh->si, C.W.scr, C.sh->lperm);
+  const int info = block_lu<T>(C.W.P, n, C.W.perm, C.lu_smem, C.sh->si, C.W.scr, C.sh->lperm,
+                               sizeof(T) == 4 ? &C.sh->tc : nullptr);
+  lu_diag_inverses<T>(C.W.P, n, C.W.dinv, (T*)C.lu_smem);
+  __syncthreads();
   ph_end(C.sh->ms, PH_LU);
   return info != 0;
 }
@@ -193,14 +190,22 @@ __device__ int dv_nlsd(Ctx<T>& C, int nflag) {
       __syncthreads();
       lin_solve<T>(C, C.y);
       if (tid == 0) d.nni++;
-      if (fabs(d.rc - 1.0) > 0.0) {
-        const double cs = 2.0 / (1.0 + d.rc);
-        for (int i = tid; i < n; i += NT) C.y[i] = cs * C.y[i];
-      }
-      const double del = bnorm(C.y, C.ewt, n, C.sh->red);
-      for (int i = tid; i < n; i += NT) {
-        C.acor[i] = C.acor[i] + C.y[i];
-        C.y[i] = yh[i] + C.acor[i];
+      double del;
+      {
+        // scale by 2/(1+rc) when rc != 1, weighted norm of the correction,
+        // acor += correction, y = yh0 + acor: one pass, one reduction
+        const bool scale = fabs(d.rc - 1.0) > 0.0;
+        const double cs = scale ? 2.0 / (1.0 + d.rc) : 1.0;
+        double ss = 0.0;
+        for (int i = tid; i < n; i += NT) {
+          const double yi = scale ? cs * C.y[i] : C.y[i];
+          const double t = yi * C.ewt[i];
+          ss += t * t;
+          const double a = C.acor[i] + yi;
+          C.acor[i] = a;
+          C.y[i] = yh[i] + a;
+        }
+        del = sqrt(block_sum<NT>(ss, C.sh->red) / n);
       }
       if (tid == 0) {
         if (d.m != 0) d.crate = fmax(0.3 * d.crate, del / d.delp);

@@ -472,6 +472,22 @@ static int build_tables(const ucl_network* net, const Consts& K, DeviceTables& T
   D.nchunk = (int)ch_row.size();
   T.nchunk = D.nchunk;
   std::vector<float> st_coef(scoef.begin(), scoef.end());
+  // packed forms (field widths checked)
+  std::vector<unsigned> fpack(nr), chpack(D.nchunk), stpack(srx.size()), rowch(n, 0u);
+  for (int j = 0; j < nr; j++) {
+    if (fya[j] < 0 || fya[j] >= 0x3FFF || fyb[j] + 1 >= 0x3FFF || fsh[j] >= 16) return UCL_E_NET;
+    fpack[j] = (unsigned)fsh[j] << 28 | (unsigned)(fyb[j] + 1) << 14 | (unsigned)fya[j];
+  }
+  if (srx.size() >= 0x10000 || D.nchunk >= 0x10000 || n >= 1024) return UCL_E_NET;
+  for (int c = 0; c < D.nchunk; c++) {
+    chpack[c] = (unsigned)ch_row[c] << 20 | (unsigned)(ch_end[c] - ch_beg[c]) << 16 | (unsigned)ch_beg[c];
+    if (c == 0 || ch_row[c - 1] != ch_row[c]) rowch[ch_row[c]] = (unsigned)c;
+    rowch[ch_row[c]] += 1u << 16;
+  }
+  for (size_t e = 0; e < srx.size(); e++) {
+    if (scoef[e] < -128 || scoef[e] > 127 || srx[e] >= 0x10000) return UCL_E_NET;
+    stpack[e] = ((unsigned)scoef[e] & 0xFFu) << 16 | (unsigned)srx[e];
+  }
   // stoichiometric coefficient lookup per (row, reaction) incl. the SURFACE total
   std::vector<std::map<int, int>> rowc(n);
   for (int i = 0; i < ns; i++)
@@ -508,6 +524,31 @@ static int build_tables(const ucl_network* net, const Consts& K, DeviceTables& T
     je_end.push_back((int)jc_key.size());
   }
   D.n_jent = (int)je_row.size();
+  // the same entries as chunks of <= 8 contributions (a few entries, e.g. the
+  // density column, have hundreds), packed one word per item:
+  //   jent[e]  = nchunks << 16 | first chunk
+  //   jchunk[c] = len << 16 | first contribution
+  //   jcpack[k] = (coef & 0xff) << 16 | (reaction << 3 | slot)
+  std::vector<unsigned> jent, jchunk, jcpack;
+  {
+    const int JCH = 8;
+    if (jc_key.size() >= 0x10000) return UCL_E_NET;
+    for (size_t e = 0; e < je_row.size(); e++) {
+      const unsigned first = (unsigned)jchunk.size();
+      for (int b = je_beg[e]; b < je_end[e]; b += JCH)
+        jchunk.push_back((unsigned)std::min(JCH, je_end[e] - b) << 16 | (unsigned)b);
+      jent.push_back(((unsigned)jchunk.size() - first) << 16 | first);
+    }
+    if (jchunk.size() >= 0x10000) return UCL_E_NET;
+    for (size_t k = 0; k < jc_key.size(); k++) {
+      const int cf = (int)jc_coef[k];
+      if ((float)cf != jc_coef[k] || cf < -128 || cf > 127 || jc_key[k] >= 0x10000) return UCL_E_NET;
+      jcpack.push_back(((unsigned)cf & 0xFFu) << 16 | (unsigned)jc_key[k]);
+    }
+  }
+  D.njch = (int)jchunk.size();
+  D.npart = std::max(D.nchunk, D.njch);
+  T.nchunk = D.npart;
   // surface-swap rank-1 rows
   std::vector<int> ar_row, ar_beg, ar_end, ar_rx;
   std::vector<float> ar_coef;
@@ -579,12 +620,19 @@ static int build_tables(const ucl_network* net, const Consts& K, DeviceTables& T
   std::vector<int> srxv(srx.begin(), srx.end());
   img.add(D.st_rx, srxv);
   img.add(D.st_coef, st_coef);
+  img.add(D.fpack, fpack);
+  img.add(D.chpack, chpack);
+  img.add(D.stpack, stpack);
+  img.add(D.rowch, rowch);
   img.add(D.je_row, je_row);
   img.add(D.je_col, je_col);
   img.add(D.je_beg, je_beg);
   img.add(D.je_end, je_end);
   img.add(D.jc_key, jc_key);
   img.add(D.jc_coef, jc_coef);
+  img.add(D.jent, jent);
+  img.add(D.jchunk, jchunk);
+  img.add(D.jcpack, jcpack);
   img.add(D.ar_row, ar_row);
   img.add(D.ar_beg, ar_beg);
   img.add(D.ar_end, ar_end);
@@ -638,7 +686,7 @@ struct ucl_ctx {
 template <typename T>
 static size_t slot_bytes(int n, int nreac) {
   return (size_t)nreac * 8 + 2 * (size_t)n * n * sizeof(T) + (size_t)n * 4 +
-         (size_t)2 * LuCfg<T>::NB * n * sizeof(T) + 4 * 256;
+         (size_t)2 * LuCfg<T>::NB * n * sizeof(T) + dinv_elems(n) * sizeof(T) + 5 * 256;
 }
 
 template <typename T>
@@ -725,8 +773,9 @@ static int solve_dev(ucl_ctx* c, int nmodels, const ucl_model_params* params_d, 
   auto a256 = [](size_t x) { return (x + 255) / 256 * 256; };
   const size_t yh_b = 256, rate_b = a256((size_t)nslots * c->nreac * 8),
                j_b = a256((size_t)nslots * n * n * sizeof(T)), perm_b = a256((size_t)nslots * n * 4),
-               scr_b = a256((size_t)nslots * 2 * LuCfg<T>::NB * n * sizeof(T));
-  int rc = c->ws.ensure(yh_b + rate_b + 2 * j_b + perm_b + scr_b + 256);
+               scr_b = a256((size_t)nslots * 2 * LuCfg<T>::NB * n * sizeof(T)),
+               dinv_b = a256((size_t)nslots * dinv_elems(n) * sizeof(T));
+  int rc = c->ws.ensure(yh_b + rate_b + 2 * j_b + perm_b + scr_b + dinv_b + 256);
   if (rc) return rc;
   char* base = (char*)c->ws.p;
   SlotArrays<T> A;
@@ -736,7 +785,8 @@ static int solve_dev(ucl_ctx* c, int nmodels, const ucl_model_params* params_d, 
   A.P = (T*)(base + yh_b + rate_b + j_b);
   A.perm = (int*)(base + yh_b + rate_b + 2 * j_b);
   A.scr = (T*)(base + yh_b + rate_b + 2 * j_b + perm_b);
-  int* counter = (int*)(base + yh_b + rate_b + 2 * j_b + perm_b + scr_b);
+  A.dinv = (T*)(base + yh_b + rate_b + 2 * j_b + perm_b + scr_b);
+  int* counter = (int*)(base + yh_b + rate_b + 2 * j_b + perm_b + scr_b + dinv_b);
   if (cudaMemsetAsync(counter, 0, sizeof(int), c->stream) != cudaSuccess) return UCL_E_CUDA;
   const SmemLayout L = smem_layout<T>(n, c->nreac, c->tab.nchunk);
   k_solve_models<T><<<nslots, NT, L.total, c->stream>>>(c->tab.dn, params_d, start_d, nmodels, max_rows, phys_d,

@@ -448,11 +448,27 @@ __device__ void dev_rhs(const DevNet& N, const ucl_model_params& P, const SysPhy
       }
     }
   } else {
-    for (int r = tid - 64; r < N.nreac; r += NT - 64) {
-      const int sh = N.fshape[r];
-      if (sh == SH_Y_TS_SM) continue;
-      const int b = N.fyb[r];
-      flux[r] = flux_of(sh, rate[r], D, y[N.fya[r]], b >= 0 ? y[b] : 0.0, R);
+    // U reactions per thread per round, all table and rate loads first
+    constexpr int U = 9;
+    constexpr int NTF = NT - 64;
+    for (int r0 = tid - 64; r0 < N.nreac; r0 += U * NTF) {
+      unsigned pk[U];
+      double kk[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int r = r0 + u * NTF;
+        pk[u] = r < N.nreac ? N.fpack[r] : 0u;
+        kk[u] = r < N.nreac ? rate[r] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int r = r0 + u * NTF;
+        const int sh = (int)(pk[u] >> 28);
+        if (r < N.nreac && sh != SH_Y_TS_SM) {
+          const int ya = (int)(pk[u] & 0x3FFFu), yb = (int)((pk[u] >> 14) & 0x3FFFu) - 1;
+          flux[r] = flux_of(sh, kk[u], D, y[ya], yb >= 0 ? y[yb] : 0.0, R);
+        }
+      }
     }
   }
   __syncthreads();
@@ -476,19 +492,37 @@ __device__ void dev_rhs(const DevNet& N, const ucl_model_params& P, const SysPhy
     }
   }
   __syncthreads();
-  // chunked CSR gather
-  for (int c = tid; c < N.nchunk; c += NT) {
-    double s = 0.0;
-    for (int e = N.ch_beg[c]; e < N.ch_end[c]; ++e) s += (double)N.st_coef[e] * flux[N.st_rx[e]];
-    part[c] = s;
+  // chunked CSR gather: two chunks per thread per round, the <= 2 x 12
+  // entry words loaded before any flux is read
+  constexpr int CHMAX = 12;
+  for (int c0 = tid; c0 < N.nchunk; c0 += 2 * NT) {
+    unsigned cp[2], e[2][CHMAX];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) cp[u] = c0 + u * NT < N.nchunk ? N.chpack[c0 + u * NT] : 0u;
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int beg = (int)(cp[u] & 0xFFFFu), len = (int)((cp[u] >> 16) & 0xFu);
+#pragma unroll
+      for (int j = 0; j < CHMAX; ++j) e[u][j] = j < len ? N.stpack[beg + j] : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int len = (int)((cp[u] >> 16) & 0xFu);
+      double s = 0.0;
+#pragma unroll
+      for (int j = 0; j < CHMAX; ++j)
+        if (j < len) s += (double)(signed char)(e[u][j] >> 16) * flux[e[u][j] & 0xFFFFu];
+      if (c0 + u * NT < N.nchunk) part[c0 + u * NT] = s;
+    }
   }
   __syncthreads();
-  for (int c = tid; c < N.nchunk; c += NT) {
-    if (c == 0 || N.ch_row[c - 1] != N.ch_row[c]) {
-      double s = part[c];
-      for (int c2 = c + 1; c2 < N.nchunk && N.ch_row[c2] == N.ch_row[c]; ++c2) s += part[c2];
-      ydot[N.ch_row[c]] = s;
-    }
+  // row sums of the chunk partials, in chunk order (rows without terms: 0)
+  for (int i = tid; i < N.neq; i += NT) {
+    const unsigned rc = N.rowch[i];
+    const int c = (int)(rc & 0xFFFFu), cnt = (int)(rc >> 16);
+    double s = 0.0;
+    for (int k = 0; k < cnt; ++k) s = k == 0 ? part[c] : s + part[c + k];
+    ydot[i] = s;
   }
   __syncthreads();
   // surface <-> bulk transfer (odes.f90:4815-5180)
@@ -531,12 +565,24 @@ __device__ void dev_rhs(const DevNet& N, const ucl_model_params& P, const SysPhy
 template <bool SCALED, typename T>
 __device__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhys& S, const double* y,
                         const double* rate, const double* w, const double* wi, T* J, const double* flux,
-                        double* dfa, double* dfb, double* vec, const RhsScal& R) {
-  const int tid = threadIdx.x;
+                        double* dfa, double* dfb, double* vec, double* jpart, const RhsScal& R) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int n = N.neq;
   const size_t nn = (size_t)n * n;
   const double D = R.D, ism = R.ism;
-  for (size_t i = tid; i < nn; i += NT) J[i] = (T)0;
+  {
+    // zero J with 16-byte stores (n*n is a multiple of the vector width)
+    using V = typename Vec2<T>::type;
+    constexpr int W = Vec2<T>::W;
+    V z;
+    T* ze = reinterpret_cast<T*>(&z);
+#pragma unroll
+    for (int q = 0; q < W; ++q) ze[q] = (T)0;
+    V* Jv = reinterpret_cast<V*>(J);
+    const size_t nv = ((uintptr_t)J & 15) == 0 ? nn / W : 0;
+    for (size_t i = tid; i < nv; i += NT) Jv[i] = z;
+    for (size_t i = nv * W + tid; i < nn; i += NT) J[i] = (T)0;
+  }
   for (int r = tid; r < N.nreac; r += NT) {
     const int sh = N.fshape[r];
     const double k = (r == N.rx_h2hv) ? R.kh2 : (r == N.rx_cohv) ? R.kco : rate[r];
@@ -562,22 +608,50 @@ __device__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhy
   const double invD = 1.0 / D;
   const double dsm = R.sm_on ? -ism : 0.0;
   const double dblr = R.blr_on ? -R.isb : 0.0;
-  for (int e = tid; e < N.n_jent; e += NT) {
-    double v = 0.0;
-    for (int c = N.je_beg[e]; c < N.je_end[e]; ++c) {
-      const int key = N.jc_key[c];
-      const int r = key >> 3, slot = key & 7;
-      double d;
-      switch (slot) {
-        case 0: d = dfa[r]; break;
-        case 1: d = dfb[r]; break;
-        case 2: d = flux[r] * invD; break;
-        case 3: d = flux[r] * dsm; break;
-        default: d = flux[r] * dblr; break;
-      }
-      v += (double)N.jc_coef[c] * d;
+  // structural entries: partial sums per chunk of <= 8 contributions (two
+  // chunks per thread per round, every table word loaded before use) ...
+  constexpr int JCH = 8;
+  for (int c0 = tid; c0 < N.njch; c0 += 2 * NT) {
+    unsigned cw[2], e[2][JCH];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) cw[u] = c0 + u * NT < N.njch ? N.jchunk[c0 + u * NT] : 0u;
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int beg = (int)(cw[u] & 0xFFFFu), len = (int)(cw[u] >> 16);
+#pragma unroll
+      for (int j = 0; j < JCH; ++j) e[u][j] = j < len ? N.jcpack[beg + j] : 0u;
     }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int len = (int)(cw[u] >> 16);
+      double v = 0.0;
+#pragma unroll
+      for (int j = 0; j < JCH; ++j) {
+        if (j < len) {
+          const int key = (int)(e[u][j] & 0xFFFFu);
+          const int r = key >> 3, slot = key & 7;
+          double d;
+          switch (slot) {
+            case 0: d = dfa[r]; break;
+            case 1: d = dfb[r]; break;
+            case 2: d = flux[r] * invD; break;
+            case 3: d = flux[r] * dsm; break;
+            default: d = flux[r] * dblr; break;
+          }
+          v += (double)(signed char)(e[u][j] >> 16) * d;
+        }
+      }
+      if (c0 + u * NT < N.njch) jpart[c0 + u * NT] = v;
+    }
+  }
+  __syncthreads();
+  // ... then one thread per entry sums its chunks and stores the entry
+  for (int e = tid; e < N.n_jent; e += NT) {
+    const unsigned ew = N.jent[e];
     const int i = N.je_row[e], j = N.je_col[e];
+    const int c = (int)(ew & 0xFFFFu), cnt = (int)(ew >> 16);
+    double v = 0.0;
+    for (int k = 0; k < cnt; ++k) v = k == 0 ? jpart[c] : v + jpart[c + k];
     if (SCALED) J[(size_t)(i) * n + j] = (T)(v * w[i] * wi[j]);
     else J[(size_t)(i) * n + j] = (T)v;
   }
@@ -645,20 +719,35 @@ __device__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhy
     uk[k] = (T)(k < ns ? -u : u);
   }
   __syncthreads();
-  for (int k = 0; k < 2 * ns; ++k) {
-    const int kk = k < ns ? k : k - ns;
-    const int row = k < ns ? N.surface_list[kk] : N.bulk_list[kk];
-    const T u = uk[k];
-    T* Jr = J + (size_t)row * n;
-    for (int j = tid; j < n; j += NT) Jr[j] += u * g[j];
+  // a warp per ice row, lanes over columns; two rows in flight per warp
+  for (int k = warp; k < 2 * ns; k += 2 * NWARP) {
+    T* Jr[2];
+    T u[2];
+    bool on[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int kq = k + h * NWARP;
+      on[h] = kq < 2 * ns;
+      const int kk = kq < ns ? kq : kq - ns;
+      const int row = on[h] ? (kq < ns ? N.surface_list[kk] : N.bulk_list[kk]) : 0;
+      u[h] = on[h] ? uk[kq] : (T)0;
+      Jr[h] = J + (size_t)row * n;
+    }
+    for (int j = lane; j < n; j += 32) {
+      const T gj = g[j];
+      T a0 = on[0] ? Jr[0][j] : (T)0;
+      T a1 = on[1] ? Jr[1][j] : (T)0;
+      if (on[0]) Jr[0][j] = a0 + u[0] * gj;
+      if (on[1]) Jr[1][j] = a1 + u[1] * gj;
+    }
   }
   __syncthreads();
-  if (tid == 0) {
-    // derivative of the coefficients: sparse entries
+  {
+    // derivative of the coefficients: sparse entries, one ice pair per
+    // thread (rows differ between pairs)
     const bool use_sm = R.neg && (R.sb * R.ism < 1.0);
-    double dsum_col = 0.0;  // sum_k dc_k / d(SURFACE or BULK)
     const int colx = use_sm ? N.nsurf : N.nbulk;
-    for (int k = 0; k < ns; ++k) {
+    for (int k = tid; k < ns; k += NT) {
       const int si = N.surface_list[k], bi = N.bulk_list[k];
       double dself, dx = 0.0;
       int jself;
@@ -670,7 +759,6 @@ __device__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhy
         jself = si;
         dself = R.sc;
       }
-      dsum_col += dx;
       const double v1 = y335 * dself, v2 = y335 * dx;
       if (SCALED) {
         J[(size_t)(si) * n + jself] -= (T)(v1 * w[si] * wi[jself]);
@@ -684,12 +772,12 @@ __device__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhy
         J[(size_t)(bi) * n + colx] += (T)v2;
       }
     }
-    vec[1000] = dsum_col;
   }
   __syncthreads();
   // SURFACE / BULK rows after transfer: sums of the ice rows
   for (int j = tid; j < n; j += NT) {
     double ssum = 0.0, bsum = 0.0;
+#pragma unroll 8
     for (int k = 0; k < ns; ++k) {
       ssum += (double)J[(size_t)N.surface_list[k] * n + j] * (SCALED ? w[N.nsurf] * wi[N.surface_list[k]] : 1.0);
       bsum += (double)J[(size_t)N.bulk_list[k] * n + j] * (SCALED ? w[N.nbulk] * wi[N.bulk_list[k]] : 1.0);

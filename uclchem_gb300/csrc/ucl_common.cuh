@@ -36,6 +36,14 @@ enum Shape : uint8_t {
   SH_DYY = 0, SH_Y, SH_DY, SH_Y_SM, SH_YY, SH_YY_BLR, SH_Y_BLR, SH_DY_SM_Y, SH_Y_TS_SM, SH_DYY_SM,
 };
 
+// 16-byte vector type of T and its width
+template <typename T>
+struct Vec2;
+template <>
+struct Vec2<float> { using type = float4; static constexpr int W = 4; };
+template <>
+struct Vec2<double> { using type = double2; static constexpr int W = 2; };
+
 struct DevNet {
   int nspec, neq, nreac, three_phase;
   int n_surface, n_bulk, n_ice;
@@ -83,6 +91,16 @@ struct DevNet {
   const int* ch_end;
   const int* st_rx;
   const float* st_coef;
+  // the same tables packed one 32-bit word per item, so the RHS issues
+  // fewer and independent loads:
+  //   fpack[r]  = shape << 28 | (yb + 1) << 14 | ya
+  //   chpack[c] = row << 20 | len << 16 | beg       (len <= 12)
+  //   stpack[e] = (coef & 0xff) << 16 | reaction    (coef as int8)
+  //   rowch[i]  = nchunks << 16 | first chunk       (every row 0..neq-1)
+  const unsigned* fpack;
+  const unsigned* chpack;
+  const unsigned* stpack;
+  const unsigned* rowch;
   // ---- analytic Jacobian ----
   // structural entries: (row, col) with contributions (reaction<<3 | slot, coef)
   // slot 0: d/dY_a, 1: d/dY_b, 2: d/dD, 3: d/dSURFACE via safeMantle, 4: d/dBULK via blr
@@ -93,6 +111,11 @@ struct DevNet {
   const int* je_end;
   const int* jc_key;
   const float* jc_coef;
+  int njch;                // chunks of <= 8 contributions
+  int npart;               // max(nchunk, njch): partial-sum scratch per system
+  const unsigned* jent;    // nchunks << 16 | first chunk
+  const unsigned* jchunk;  // len << 16 | first contribution
+  const unsigned* jcpack;  // (coef & 0xff) << 16 | key
   // surface-swap rank-1: rows with A_i = sum_r S_ir k_r ya_r / sm over shape-8 reactions
   int n_arow;
   const int* ar_row;
@@ -135,17 +158,14 @@ template <int NTH>
 __device__ __forceinline__ double block_sum(double v, double* red) {
   v = warp_sum(v);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  __syncthreads();
+  __syncthreads();  // red may still be read by a previous call
   if (l == 0) red[w] = v;
   __syncthreads();
-  double s = 0.0;
-  if (threadIdx.x == 0) {
+  // every thread adds the warp sums in the same order (identical results)
+  double s = red[0];
 #pragma unroll
-    for (int i = 0; i < NTH / 32; ++i) s += red[i];
-    red[NTH / 32] = s;
-  }
-  __syncthreads();
-  return red[NTH / 32];
+  for (int i = 1; i < NTH / 32; ++i) s += red[i];
+  return s;
 }
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {

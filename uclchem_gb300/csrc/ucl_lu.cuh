@@ -6,15 +6,18 @@
 // the register-tiled trailing update are all coalesced.  The blocked
 // right-looking algorithm:
 //   for each panel of NB columns:
-//     factor the (n-k0) x NB panel in shared memory (warp pivot search,
-//     row swap, scaling, rank-1 updates);
-//     swap the same rows in the columns outside the panel;
+//     factor the (n-k0) x NB panel in registers (one barrier per column:
+//     warp max-reductions of |v|, candidates exchanged in shared memory);
+//     apply the panel's interchanges to the columns outside it;
 //     U12 = L11^-1 A12 (one thread per column, registers);
 //     A22 -= L21 * U12 (register tiles of TM x TN, operands in shared memory).
 // The composite row permutation is kept as perm[] so a solve gathers the
-// right-hand side in one parallel pass.
+// right-hand side in one parallel pass; the inverses of the 32 x 32 diagonal
+// blocks of L turn each forward block step into a small GEMV, and compact
+// copies of the diagonal blocks of U are solved from registers.
 #pragma once
 #include "ucl_common.cuh"
+#include "ucl_tc.cuh"
 
 namespace ucl {
 
@@ -35,12 +38,6 @@ struct LuCfg<double> {
 };
 static_assert(LuCfg<float>::NB <= LU_NB_MAX && LuCfg<double>::NB <= LU_NB_MAX, "LU scratch too small");
 
-template <typename T>
-struct Vec2;
-template <>
-struct Vec2<float> { using type = float4; static constexpr int W = 4; };
-template <>
-struct Vec2<double> { using type = double2; static constexpr int W = 2; };
 
 // P = I + con * J over an n x n row-major matrix: 16-byte vector loads issued
 // four at a time so the L2 round trips overlap.  n*n must be a multiple of
@@ -78,173 +75,290 @@ __device__ void form_newton_matrix(const T* __restrict__ J, T* __restrict__ P, i
   __syncthreads();
 }
 
+// Shared-memory layout of block_lu: the factored panel (L11/L21, rows of
+// LDP = NB+1), the U12 block row, the per-warp pivot candidates (double
+// buffered), and the panel's position maps.
+// FP32 factorisations of n <= TC_MAX_N run the trailing update on the tensor
+// cores (the staging of the split operands must fit in shared memory).
+constexpr int TC_MAX_N = 352;
+
+template <typename T>
+struct LuSmem {
+  static constexpr int NB = LuCfg<T>::NB, LDP = NB + 1;
+  __host__ __device__ static constexpr size_t al(size_t b) { return (b + 127) & ~(size_t)127; }
+  __host__ __device__ static constexpr bool tc_ok(int n) { return sizeof(T) == 4 && n <= TC_MAX_N; }
+  __host__ __device__ static constexpr int np(int n) { return (n + 15) & ~15; }
+  __host__ __device__ static constexpr size_t sp(int) { return 0; }
+  // U12 block row (CUDA-core update) or the tensor-core operand staging:
+  // A tile head, A tile tail, B head, B tail
+  __host__ __device__ static constexpr size_t su(int n) { return al((size_t)n * LDP * sizeof(T)); }
+  __host__ __device__ static constexpr size_t su_bytes(int n) {
+    return tc_ok(n) ? tc_stage_bytes(np(n)) : (size_t)NB * n * sizeof(T);
+  }
+  __host__ __device__ static constexpr size_t crow(int n) { return su(n) + al(su_bytes(n)); }
+  __host__ __device__ static constexpr size_t ckey(int n) { return crow(n) + (size_t)2 * NWARP * NB * sizeof(T); }
+  __host__ __device__ static constexpr size_t maps(int n) { return ckey(n) + (size_t)2 * NWARP * 4 * sizeof(unsigned); }
+  // (the diagonal-block inversion after the factorisation reuses the area
+  // for NWARP staged 32 x 33 tiles)
+  __host__ __device__ static constexpr size_t tiles() { return (size_t)NWARP * 32 * 33 * sizeof(T); }
+  __host__ __device__ static constexpr size_t bytes(int n) {
+    return maps(n) + al((size_t)2 * n * sizeof(int)) + 16 > tiles() ? maps(n) + al((size_t)2 * n * sizeof(int)) + 16
+                                                                     : tiles();
+  }
+};
+
 // shared-memory bytes the LU needs for an n x n matrix
 template <typename T>
 __host__ __device__ constexpr size_t lu_smem_bytes(int n) {
-  return sizeof(T) * ((size_t)n * (LuCfg<T>::NB + 1) + (size_t)LuCfg<T>::NB * n) + 64;
+  return LuSmem<T>::bytes(n);
+}
+
+// |v| as an unsigned key whose integer order is the order of |v|
+__device__ __forceinline__ unsigned long long abs_key(double v) {
+  return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
+__device__ __forceinline__ unsigned long long abs_key(float v) {
+  return (unsigned long long)(__float_as_uint(v) & 0x7fffffffu);
+}
+// warp maximum of a key (keys of floats fit in 32 bits)
+template <typename T>
+__device__ __forceinline__ unsigned long long warp_max_key(unsigned long long k) {
+  if (sizeof(T) == 4) return __reduce_max_sync(0xffffffffu, (unsigned)k);
+  const unsigned hi = __reduce_max_sync(0xffffffffu, (unsigned)(k >> 32));
+  const unsigned lo = __reduce_max_sync(0xffffffffu, (unsigned)(k >> 32) == hi ? (unsigned)k : 0u);
+  return ((unsigned long long)hi << 32) | lo;
+}
+
+// Factor the m x nb panel at (k0, k0) with partial pivoting, rows held in
+// registers: thread t owns panel rows t + NT*s (s < RPT).  Rows are not
+// moved while the panel is factored; row_at/pos_of record which row sits at
+// each position after the LINPACK-order interchanges (DGEFA's ipvt).  One
+// barrier per column: every warp publishes its best candidate (|v| key, row,
+// and the row's values) in a double-buffered slot, then every warp reduces
+// the NWARP candidates itself.  Ties go to the lowest lane / warp.  Zero
+// pivot: as DGEFA, no interchange and no elimination, info = column + 1.
+// Rows are written back to A (panel columns, final positions) and to the
+// shared panel sp for the U12 solve and the trailing update.
+template <typename T, int RPT>
+__device__ __forceinline__ int panel_factor(T* __restrict__ A, int n, int k0, int nb, int m, char* smem,
+                                            int info) {
+  constexpr int NB = LuCfg<T>::NB, LDP = NB + 1;
+  using V = typename Vec2<T>::type;
+  constexpr int W = Vec2<T>::W;
+  T* sp = (T*)(smem + LuSmem<T>::sp(n));
+  T* crow = (T*)(smem + LuSmem<T>::crow(n));              // [2][NWARP][NB]
+  unsigned* ckey = (unsigned*)(smem + LuSmem<T>::ckey(n));  // [2][NWARP][4]
+  int* row_at = (int*)(smem + LuSmem<T>::maps(n));
+  int* pos_of = row_at + n;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const bool vec = (n % W) == 0;
+  T a[RPT][NB];
+  bool done[RPT];
+#pragma unroll
+  for (int s = 0; s < RPT; ++s) {
+    const int i = tid + NT * s;
+    done[s] = i >= m;
+    const T* src = A + (size_t)(k0 + i) * n + k0;
+    if (i < m && vec && nb == NB) {
+#pragma unroll
+      for (int j = 0; j < NB; j += W) {
+        const V v = *reinterpret_cast<const V*>(src + j);
+        const T* e = reinterpret_cast<const T*>(&v);
+#pragma unroll
+        for (int w = 0; w < W; ++w) a[s][j + w] = e[w];
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < NB; ++j) a[s][j] = (i < m && j < nb) ? src[j] : (T)0;
+    }
+    if (i < m) { row_at[i] = i; pos_of[i] = i; }
+  }
+#pragma unroll
+  for (int c = 0; c < NB; ++c) {
+    if (c < nb) {
+      const int buf = c & 1;
+      // this thread's best row, then the warp's (key, row, values)
+      unsigned long long bk = 0;
+      int bs = 0;
+#pragma unroll
+      for (int s = 0; s < RPT; ++s) {
+        const unsigned long long k = done[s] ? 0ull : abs_key(a[s][c]);
+        if (k > bk) { bk = k; bs = s; }
+      }
+      const unsigned long long wk = warp_max_key<T>(bk);
+      const int owner = __ffs(__ballot_sync(0xffffffffu, bk == wk)) - 1;
+      if (lane == owner) {
+        T* dst = crow + (size_t)(buf * NWARP + warp) * NB;
+#pragma unroll
+        for (int j = c; j < NB; ++j) {
+          T v = a[0][j];
+#pragma unroll
+          for (int s = 1; s < RPT; ++s)
+            if (bs == s) v = a[s][j];
+          dst[j] = v;
+        }
+        unsigned* kk = ckey + (buf * NWARP + warp) * 4;
+        kk[0] = (unsigned)wk;
+        kk[1] = (unsigned)(wk >> 32);
+        kk[2] = (unsigned)(tid + NT * bs);
+      }
+      __syncthreads();
+      // winner over the warps
+      unsigned long long ck = 0;
+      int crow_i = 0;
+      if (lane < NWARP) {
+        const uint4 kk = *reinterpret_cast<const uint4*>(ckey + (buf * NWARP + lane) * 4);
+        ck = ((unsigned long long)kk.y << 32) | kk.x;
+        crow_i = (int)kk.z;
+      }
+      const unsigned long long mk = warp_max_key<T>(ck);
+      const int ww = __ffs(__ballot_sync(0xffffffffu, lane < NWARP && ck == mk)) - 1;
+      int pi = __shfl_sync(0xffffffffu, crow_i, ww);
+      if (mk == 0ull) {
+        // zero pivot column: the row at position c stays, nothing eliminated
+        pi = row_at[c];
+        if (info == 0) info = k0 + c + 1;
+#pragma unroll
+        for (int s = 0; s < RPT; ++s)
+          if (tid + NT * s == pi) done[s] = true;
+      } else {
+        const T* pr = crow + (size_t)(buf * NWARP + ww) * NB;
+        T prow[NB];
+        const int c0 = (c / W) * W;
+        if (NB % W == 0) {
+#pragma unroll
+          for (int j = c0; j < NB; j += W) {
+            const V v = *reinterpret_cast<const V*>(pr + j);
+            const T* e = reinterpret_cast<const T*>(&v);
+#pragma unroll
+            for (int w = 0; w < W; ++w) prow[j + w] = e[w];
+          }
+        }
+        const T inv = (T)1 / prow[c];
+#pragma unroll
+        for (int s = 0; s < RPT; ++s) {
+          if (done[s]) continue;
+          if (tid + NT * s == pi) { done[s] = true; continue; }
+          const T l = a[s][c] * inv;
+          a[s][c] = l;
+#pragma unroll
+          for (int j = c + 1; j < NB; ++j) a[s][j] -= l * prow[j];
+        }
+      }
+      if (tid == 0) {
+        const int q = pos_of[pi], r2 = row_at[c];
+        row_at[c] = pi;
+        row_at[q] = r2;
+        pos_of[pi] = c;
+        pos_of[r2] = q;
+      }
+    }
+  }
+  __syncthreads();
+  // rows to their final positions, in A and in the shared panel
+#pragma unroll
+  for (int s = 0; s < RPT; ++s) {
+    const int i = tid + NT * s;
+    if (i >= m) continue;
+    const int fp = pos_of[i];
+    T* dst = A + (size_t)(k0 + fp) * n + k0;
+    if (vec && nb == NB) {
+#pragma unroll
+      for (int j = 0; j < NB; j += W) {
+        V v;
+        T* e = reinterpret_cast<T*>(&v);
+#pragma unroll
+        for (int w = 0; w < W; ++w) e[w] = a[s][j + w];
+        *reinterpret_cast<V*>(dst + j) = v;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < NB; ++j)
+        if (j < nb) dst[j] = a[s][j];
+    }
+#pragma unroll
+    for (int j = 0; j < NB; ++j)
+      if (j < nb) sp[fp * LDP + j] = a[s][j];
+  }
+  return info;
 }
 
 // Factor A (row-major n x n, global) in place.  perm[i] = original row of
 // row i after pivoting.  Returns 0 or (first zero pivot index + 1).
+// s_i: LU_SI_INTS ints of shared scratch; scr: 2*NB*n elements of global
+// scratch for the row interchanges outside the panel; perm: shared [n].
+// tc: tensor-core state of the CTA (TMEM + mbarrier) or nullptr for the
+// CUDA-core trailing update.
 template <typename T>
 __device__ int block_lu(T* __restrict__ A, int n, int* __restrict__ perm_out, char* smem, int* s_i,
-                         T* __restrict__ scr, int* perm) {
+                         T* __restrict__ scr, int* perm, TcState* tc = nullptr) {
   constexpr int NB = LuCfg<T>::NB, TM = LuCfg<T>::TM, TN = LuCfg<T>::TN;
   constexpr int LDP = NB + 1;
-  T* sp = (T*)smem;                  // panel [m x LDP]
-  T* su = sp + (size_t)n * LDP;      // U12 [NB x ncols]
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  T* sp = (T*)(smem + LuSmem<T>::sp(n));   // panel [m x LDP]
+  T* su = (T*)(smem + LuSmem<T>::su(n));   // U12 [NB x ncols]
+  const int* row_at = (const int*)(smem + LuSmem<T>::maps(n));
+  const int tid = threadIdx.x;
   int info = 0;
-  // perm lives in shared memory while factoring (it is updated per column)
+  // perm lives in shared memory while factoring
   for (int i = tid; i < n; i += NT) perm[i] = i;
-  __syncthreads();
   for (int k0 = 0; k0 < n; k0 += NB) {
     const int nb = min(NB, n - k0);
     const int m = n - k0;
     const int ncols = n - k0 - nb;
+    if (tid == 0) s_i[39] = 0;
+    __syncthreads();
+    if (m <= NT) info = panel_factor<T, 1>(A, n, k0, nb, m, smem, info);
+    else if (m <= 2 * NT) info = panel_factor<T, 2>(A, n, k0, nb, m, smem, info);
+    else info = panel_factor<T, (MAX_NEQ + NT - 1) / NT>(A, n, k0, nb, m, smem, info);
+    // composite permutation and the list of moved rows (dst <- src), <= 2*nb
+    int* mv = s_i + 40;
+    int pv[(MAX_NEQ + NT - 1) / NT];
+#pragma unroll
+    for (int s = 0; s < (MAX_NEQ + NT - 1) / NT; ++s) {
+      const int i = tid + NT * s;
+      if (i < m) {
+        const int src = row_at[i];
+        pv[s] = perm[k0 + src];
+        if (src != i) {
+          const int q = atomicAdd(&s_i[39], 1);
+          mv[2 * q] = k0 + i;
+          mv[2 * q + 1] = k0 + src;
+        }
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < (MAX_NEQ + NT - 1) / NT; ++s)
+      if (tid + NT * s < m) perm[k0 + tid + NT * s] = pv[s];
     {
-      const int tot = m * nb;
-      int idx = tid;
-      for (; idx + 3 * NT < tot; idx += 4 * NT) {
-        T v[4];
-        int rr[4], cc[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          rr[u] = (idx + u * NT) / nb;
-          cc[u] = idx + u * NT - rr[u] * nb;
-          v[u] = A[(size_t)(k0 + rr[u]) * n + k0 + cc[u]];
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) sp[rr[u] * LDP + cc[u]] = v[u];
-      }
-      for (; idx < tot; idx += NT) {
-        const int r = idx / nb, c = idx - r * nb;
-        sp[r * LDP + c] = A[(size_t)(k0 + r) * n + k0 + c];
-      }
-    }
-    __syncthreads();
-    for (int c = 0; c < nb; ++c) {
-      if (warp == 0) {
-        T best = (T)-1;
-        int bi = c;
-        for (int r = c + lane; r < m; r += 32) {
-          const T v = fabs(sp[r * LDP + c]);
-          if (v > best) { best = v; bi = r; }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const T ov = __shfl_xor_sync(0xffffffffu, best, o);
-          const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-          if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
-        }
-        if (lane == 0) s_i[0] = bi;
-      }
-      __syncthreads();
-      const int p = s_i[0];
-      const T pv = sp[p * LDP + c];
-      if (pv == (T)0) {
-        if (info == 0) info = k0 + c + 1;
-        if (tid == 0) s_i[1 + c] = c;
-        __syncthreads();
-        continue;
-      }
-      if (p != c) {
-        for (int j = tid; j < nb; j += NT) {
-          const T t = sp[p * LDP + j];
-          sp[p * LDP + j] = sp[c * LDP + j];
-          sp[c * LDP + j] = t;
-        }
-        if (tid == 0) {
-          const int t = perm[k0 + p];
-          perm[k0 + p] = perm[k0 + c];
-          perm[k0 + c] = t;
-          s_i[1 + c] = p;  // remember the interchange for the other columns
-        }
-      } else if (tid == 0) {
-        s_i[1 + c] = c;
-      }
-      __syncthreads();
-      const T inv = (T)1 / sp[c * LDP + c];
-      T prow[NB];
-#pragma unroll
-      for (int j = 0; j < NB; ++j) prow[j] = (j > c && j < nb) ? sp[c * LDP + j] : (T)0;
-      for (int r = c + 1 + tid; r < m; r += NT) {
-        T* row = sp + r * LDP;
-        const T l = row[c] * inv;
-        row[c] = l;
-#pragma unroll
-        for (int j = 0; j < NB; ++j)
-          if (j > c && j < nb) row[j] -= l * prow[j];
-      }
-      __syncthreads();
-    }
-    // panel back to A
-    for (int idx = tid; idx < m * nb; idx += NT) {
-      const int r = idx / nb, c = idx - r * nb;
-      A[(size_t)(k0 + r) * n + k0 + c] = sp[r * LDP + c];
-    }
-    __syncthreads();
-    // the same interchanges in the columns outside the panel, applied as one
-    // gather: thread 0 composes the nb transpositions into dst <- src row
-    // pairs (s_i[40..]), then all threads stage the source rows in scr and
-    // write them back (independent, coalesced row segments).
-    int* mv_dst = s_i + 40;  // <= 2*NB moved rows
-    if (tid == 0) {
-      int cnt = 0;
-      int rows[2 * NB], src[2 * NB];
-      for (int c = 0; c < nb; ++c) {
-        const int a = k0 + c, b = k0 + s_i[1 + c];
-        if (a == b) continue;
-        int ia = -1, ib = -1;
-        for (int q = 0; q < cnt; ++q) { if (rows[q] == a) ia = q; if (rows[q] == b) ib = q; }
-        if (ia < 0) { rows[cnt] = a; src[cnt] = a; ia = cnt++; }
-        if (ib < 0) { rows[cnt] = b; src[cnt] = b; ib = cnt++; }
-        const int t = src[ia]; src[ia] = src[ib]; src[ib] = t;
-      }
-      int m2 = 0;
-      for (int q = 0; q < cnt; ++q)
-        if (src[q] != rows[q]) { mv_dst[2 * m2] = rows[q]; mv_dst[2 * m2 + 1] = src[q]; ++m2; }
-      s_i[39] = m2;
-    }
-    __syncthreads();
-    {
+      // the same interchanges in the columns outside the panel, as one
+      // gather through scr: a warp per moved row, 16-byte row segments
+      using V = typename Vec2<T>::type;
+      constexpr int W = Vec2<T>::W;
+      const int lane = tid & 31, warp = tid >> 5;
       const int m2 = s_i[39];
-      const int w = n - nb;  // columns outside the panel
-      const int tot = m2 * w;
-      for (int idx = tid; idx < tot; idx += 4 * NT) {
-        T v[4];
-        size_t dst[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int id = idx + u * NT;
-          const int q = id / w, jj0 = id - q * w;
-          const int jj = jj0 < k0 ? jj0 : jj0 + nb;
-          dst[u] = (size_t)q * n + jj;
-          v[u] = id < tot ? A[(size_t)mv_dst[2 * q + 1] * n + jj] : (T)0;
+      const bool vec = (n % W) == 0;
+      for (int pass = 0; pass < 2; ++pass) {
+        for (int q = warp; q < m2; q += NWARP) {
+          const T* src = pass == 0 ? A + (size_t)mv[2 * q + 1] * n : scr + (size_t)q * n;
+          T* dst = pass == 0 ? scr + (size_t)q * n : A + (size_t)mv[2 * q] * n;
+          if (vec) {
+            for (int j = lane * W; j < n; j += 32 * W)
+              if (j < k0 || j >= k0 + nb)
+                *reinterpret_cast<V*>(dst + j) = *reinterpret_cast<const V*>(src + j);
+          } else {
+            for (int j = lane; j < n; j += 32)
+              if (j < k0 || j >= k0 + nb) dst[j] = src[j];
+          }
         }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-          if (idx + u * NT < tot) scr[dst[u]] = v[u];
-      }
-      __syncthreads();
-      for (int idx = tid; idx < tot; idx += 4 * NT) {
-        T v[4];
-        size_t dst[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int id = idx + u * NT;
-          const int q = id / w, jj0 = id - q * w;
-          const int jj = jj0 < k0 ? jj0 : jj0 + nb;
-          dst[u] = (size_t)mv_dst[2 * q] * n + jj;
-          v[u] = id < tot ? scr[(size_t)q * n + jj] : (T)0;
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-          if (idx + u * NT < tot) A[dst[u]] = v[u];
+        __syncthreads();
       }
     }
     __syncthreads();
     if (ncols > 0) {
+      const bool use_tc = tc != nullptr && LuSmem<T>::tc_ok(n) && nb == NB;
+      char* bh = (char*)su + 2 * TC_M * 128;
+      char* bl = bh + (size_t)LuSmem<T>::np(ncols) * 128;
       // U12 = L11^-1 A12
       for (int jj = tid; jj < ncols; jj += NT) {
         T x[NB];
@@ -257,14 +371,37 @@ __device__ int block_lu(T* __restrict__ A, int n, int* __restrict__ perm_out, ch
           }
         }
 #pragma unroll
-        for (int q = 0; q < NB; ++q) {
-          if (q < nb) {
-            A[(size_t)(k0 + q) * n + k0 + nb + jj] = x[q];
-            su[q * ncols + jj] = x[q];
+        for (int q = 0; q < NB; ++q)
+          if (q < nb) A[(size_t)(k0 + q) * n + k0 + nb + jj] = x[q];
+        if constexpr (sizeof(T) == 4) {
+          if (use_tc) {
+            // B operand of the tensor-core update: row jj = column jj of U12
+#pragma unroll
+            for (int q = 0; q < NB; q += 4) tc_put4(bh, bl, jj, q, x[q], x[q + 1], x[q + 2], x[q + 3]);
+            continue;
           }
+        }
+#pragma unroll
+        for (int q = 0; q < NB; ++q)
+          if (q < nb) su[q * ncols + jj] = x[q];
+      }
+      if (use_tc) {
+        // zero rows of B past ncols (N is padded to a multiple of 16)
+        for (int t = tid; t < (LuSmem<T>::np(ncols) - ncols) * 8; t += NT) {
+          const int r = ncols + (t >> 3), k4 = (t & 7) * 4;
+          tc_put4(bh, bl, r, k4, 0.f, 0.f, 0.f, 0.f);
         }
       }
       __syncthreads();
+      if constexpr (sizeof(T) == 4) {
+        if (use_tc) {
+          if (!tc_trailing_update(A, n, k0 + nb, k0 + nb, m - nb, ncols, sp + nb * LDP, LDP, (char*)su,
+                                  (char*)su + TC_M * 128, bh, bl, tc))
+            info = n + 1;
+          __syncthreads();
+          continue;
+        }
+      }
       // A22 -= L21 * U12
       const int R = m - nb;
       const int TR = (R + TM - 1) / TM, TC = (ncols + TN - 1) / TN;
@@ -344,91 +481,155 @@ __device__ int block_lu(T* __restrict__ A, int n, int* __restrict__ perm_out, ch
   return info;
 }
 
-// s - row[0:nb] . x[0:nb], with 16-byte loads of the row when aligned
+// elements of the diagonal-block inverses of an n x n factorisation
+__host__ __device__ constexpr size_t dinv_elems(int n) { return (size_t)((n + 31) / 32) * 2 * 1024; }
+
+// Diagonal 32 x 32 blocks of the factors in the form the block solves use,
+// after block_lu: dinv[(2*b + 0)*1024 + i*32 + j] = (L_bb^-1)[i][j] (unit
+// lower, |l| <= 1, so its inverse is well conditioned), and
+// dinv[(2*b + 1)*1024 + ...] = U_bb itself (upper part, contiguous) with the
+// reciprocal of the pivot on the diagonal: U blocks carry the conditioning
+// of P, so they are applied by substitution, which is backward stable (an
+// explicit U_bb^-1 measurably loosened element conservation of the FP32
+// solve).  Rows and columns past n are the identity.  One warp per block:
+// lane j forms column j of L_bb^-1 by substitution against the block staged
+// in shared memory.  tile: shared, NWARP * 32 * 33 elements.
 template <typename T>
-__device__ __forceinline__ T dot_sub(const T* __restrict__ row, const T* x, int nb, T s, int n) {
-  using V = typename Vec2<T>::type;
-  constexpr int W = Vec2<T>::W;
-  if ((n % W) == 0 && (nb % W) == 0) {
-    const V* rv = reinterpret_cast<const V*>(row);
-    V buf[32 / W];
+__device__ void lu_diag_inverses(const T* __restrict__ A, int n, T* __restrict__ dinv, T* tile) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nblk = (n + 31) / 32;
+  T* t = tile + warp * 32 * 33;
+  for (int job = warp; job < 2 * nblk; job += NWARP) {
+    const int b = job >> 1, k0 = b * 32, nb = min(32, n - k0);
+    const bool upper = job & 1;
+#pragma unroll 8
+    for (int r = 0; r < 32; ++r)
+      t[r * 33 + lane] = (r < nb && lane < nb) ? A[(size_t)(k0 + r) * n + k0 + lane] : (T)(r == lane ? 1 : 0);
+    __syncwarp();
+    T y[32];
+    if (!upper) {
 #pragma unroll
-    for (int u = 0; u < 32 / W; ++u)
-      if (u * W < nb) buf[u] = rv[u];
+      for (int i = 0; i < 32; ++i) {
+        T v = (i == lane) ? (T)1 : (T)0;
 #pragma unroll
-    for (int u = 0; u < 32 / W; ++u)
-      if (u * W < nb) {
-        const T* e = reinterpret_cast<const T*>(&buf[u]);
-#pragma unroll
-        for (int w = 0; w < W; ++w) s -= e[w] * x[u * W + w];
+        for (int q = 0; q < i; ++q) v -= t[i * 33 + q] * y[q];
+        y[i] = v;
       }
-    return s;
+    } else {
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        const T u = t[i * 33 + lane];
+        y[i] = lane > i ? u : lane == i ? (T)1 / u : (T)0;
+      }
+    }
+    T* d = dinv + (size_t)job * 1024;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) d[i * 32 + lane] = y[i];
+    __syncwarp();
   }
-  for (int q = 0; q < nb; ++q) s -= row[q] * x[q];
-  return s;
 }
 
-// Solve (LU) x = b in place, x in shared memory (precision T), perm from
-// block_lu.  tmp: shared [n]; tile: shared [32 x 33] staging of the diagonal
-// blocks.  Per 32-row block: warp 0 solves the diagonal block from the
-// staged tile while the others wait; then all threads update the remaining
-// rows (16-byte row loads) and, in the same phase, stage the next diagonal
-// block, so the two load latencies overlap.
+// Solve (LU) x = b with the factors, the row permutation and the diagonal
+// blocks prepared by lu_diag_inverses.
+// Forward over the 32-row blocks of L, then backward over those of U; per
+// block: r = b_blk - (off-diagonal block row) . x with 4 rows per warp,
+// lane-strided 16-byte loads (independent of x, so they are all in flight
+// at once) and warp sums; then warp 0 forms x_blk = L_bb^-1 r (a GEMV) or
+// solves U_bb x_blk = r from registers.  Two barriers per block.
+// tmp: shared [n]; rbuf: shared [32].
+// The right-hand side comes in and the solution goes out as FP64 y (shared):
+// the system solved is (LU) x = W y and y <- W^-1 x, with W = diag(ws) and
+// W^-1 = diag(wis) (both nullptr: no scaling).
 template <typename T>
-__device__ void block_lusolve(const T* __restrict__ A, int n, const int* __restrict__ perm, T* x,
-                                           T* tmp, T* tile) {
+__device__ void block_lusolve(const T* __restrict__ A, int n, const int* __restrict__ perm,
+                              const T* __restrict__ dinv, double* y, const double* ws, const double* wis, T* tmp,
+                              T* rbuf) {
+  using V = typename Vec2<T>::type;
+  constexpr int W = Vec2<T>::W;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nblk = (n + 31) / 32;
-  auto stage = [&](int k0, bool upper) {
-    const int nb = min(32, n - k0);
-    for (int idx = tid; idx < 32 * 32; idx += NT) {
-      const int r = idx >> 5, c = idx & 31;
-      const bool in = r < nb && c < nb && (upper ? c >= r : c < r);
-      tile[r * 33 + c] = in ? A[(size_t)(k0 + r) * n + k0 + c] : (T)0;
-    }
-  };
-  for (int i = tid; i < n; i += NT) tmp[i] = x[perm[i]];
-  stage(0, false);
-  __syncthreads();
-  // forward: unit lower
-  for (int bk = 0; bk < nblk; ++bk) {
-    const int k0 = bk * 32, nb = min(32, n - k0);
-    if (warp == 0) {
-      T xi = lane < nb ? tmp[k0 + lane] : (T)0;
-#pragma unroll
-      for (int q = 0; q < 31; ++q) {
-        const T xq = __shfl_sync(0xffffffffu, xi, q);
-        if (lane > q) xi -= tile[lane * 33 + q] * xq;
-      }
-      if (lane < nb) tmp[k0 + lane] = xi;
-    }
-    __syncthreads();
-    for (int i = k0 + nb + tid; i < n; i += NT) tmp[i] = dot_sub<T>(A + (size_t)i * n + k0, tmp + k0, nb, tmp[i], n);
-    if (bk + 1 < nblk) stage(k0 + 32, false);
-    else stage((nblk - 1) * 32, true);
-    __syncthreads();
+  const bool vec = (n % W) == 0;
+  for (int i = tid; i < n; i += NT) {
+    const int p = perm[i];
+    tmp[i] = (T)(ws ? ws[p] * y[p] : y[p]);
   }
-  // backward: upper
-  for (int bk = nblk - 1; bk >= 0; --bk) {
-    const int k0 = bk * 32, nb = min(32, n - k0);
-    if (warp == 0) {
-      T xi = lane < nb ? tmp[k0 + lane] : (T)0;
+  __syncthreads();
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int step = 0; step < nblk; ++step) {
+      const int b = pass == 0 ? step : nblk - 1 - step;
+      const int k0 = b * 32, nb = min(32, n - k0);
+      const int c0 = pass == 0 ? 0 : k0 + nb, c1 = pass == 0 ? k0 : n;
+      T drow[32];
+      if (warp == 0) {
+        const V* dv = reinterpret_cast<const V*>(dinv + (size_t)(2 * b + pass) * 1024 + lane * 32);
 #pragma unroll
-      for (int q = 31; q >= 0; --q) {
-        if (q < nb) {
-          if (lane == q) xi = xi / tile[q * 33 + q];
-          const T xq = __shfl_sync(0xffffffffu, xi, q);
-          if (lane < q) xi -= tile[lane * 33 + q] * xq;
+        for (int u = 0; u < 32 / W; ++u) {
+          const V v = dv[u];
+          const T* e = reinterpret_cast<const T*>(&v);
+#pragma unroll
+          for (int w = 0; w < W; ++w) drow[u * W + w] = e[w];
         }
       }
-      if (lane < nb) tmp[k0 + lane] = xi;
+      T s[4] = {(T)0, (T)0, (T)0, (T)0};
+      const int r0 = warp * 4;
+      if (vec) {
+        // c0, c1 are multiples of W here (block edges, n % W == 0)
+        for (int j = c0 + lane * W; j < c1; j += 32 * W) {
+          const V xv = *reinterpret_cast<const V*>(tmp + j);
+          const T* xe = reinterpret_cast<const T*>(&xv);
+          V av[4];
+#pragma unroll
+          for (int a = 0; a < 4; ++a)
+            if (r0 + a < nb) av[a] = *reinterpret_cast<const V*>(A + (size_t)(k0 + r0 + a) * n + j);
+#pragma unroll
+          for (int a = 0; a < 4; ++a)
+            if (r0 + a < nb) {
+              const T* e = reinterpret_cast<const T*>(&av[a]);
+#pragma unroll
+              for (int w = 0; w < W; ++w) s[a] += e[w] * xe[w];
+            }
+        }
+      } else {
+        for (int j = c0 + lane; j < c1; j += 32) {
+          const T xj = tmp[j];
+#pragma unroll
+          for (int a = 0; a < 4; ++a)
+            if (r0 + a < nb) s[a] += A[(size_t)(k0 + r0 + a) * n + j] * xj;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int a = 0; a < 4; ++a) s[a] += __shfl_xor_sync(0xffffffffu, s[a], o);
+      if (lane < 4) {
+        const int r = r0 + lane;
+        const T sv = lane == 0 ? s[0] : lane == 1 ? s[1] : lane == 2 ? s[2] : s[3];
+        rbuf[r] = r < nb ? tmp[k0 + r] - sv : (T)0;
+      }
+      __syncthreads();
+      if (warp == 0) {
+        T v;
+        if (pass == 0) {
+          v = (T)0;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) v += drow[j] * rbuf[j];
+        } else {
+          // back substitution on the block held in registers (drow = row
+          // `lane` of U_bb, reciprocal pivot on the diagonal)
+          v = rbuf[lane];
+#pragma unroll
+          for (int q = 31; q >= 0; --q) {
+            if (lane == q) v *= drow[q];
+            const T xq = __shfl_sync(0xffffffffu, v, q);
+            if (lane < q) v -= drow[q] * xq;
+          }
+        }
+        if (lane < nb) tmp[k0 + lane] = v;
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    for (int i = tid; i < k0; i += NT) tmp[i] = dot_sub<T>(A + (size_t)i * n + k0, tmp + k0, nb, tmp[i], n);
-    if (bk > 0) stage(k0 - 32, true);
-    __syncthreads();
   }
-  for (int i = tid; i < n; i += NT) x[i] = tmp[i];
+  for (int i = tid; i < n; i += NT) y[i] = wis ? (double)tmp[i] * wis[i] : (double)tmp[i];
   __syncthreads();
 }
 

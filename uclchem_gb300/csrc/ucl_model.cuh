@@ -288,6 +288,7 @@ struct SlotArrays {
   T* P;
   int* perm;
   T* scr;
+  T* dinv;
 };
 
 template <typename T>
@@ -299,6 +300,7 @@ __device__ __forceinline__ Slot<T> slot_of(const SlotArrays<T>& A, int s, int n,
   W.P = A.P + (size_t)s * n * n;
   W.perm = A.perm + (size_t)s * n;
   W.scr = A.scr + (size_t)s * 2 * LuCfg<T>::NB * n;
+  W.dinv = A.dinv + (size_t)s * dinv_elems(n);
   return W;
 }
 
@@ -312,9 +314,10 @@ __global__ void __launch_bounds__(NT, 1) k_solve_models(DevNet N, const ucl_mode
   __shared__ Shared sh;
   __shared__ DevNet sN;
   if (threadIdx.x == 0) sN = N;
-  const SmemLayout L = smem_layout<T>(N.neq, N.nreac, N.nchunk);
+  const SmemLayout L = smem_layout<T>(N.neq, N.nreac, N.npart);
   __syncthreads();
   Ctx<T> C = make_ctx<T>(&sN, &sh, smem, L, slot_of(ws, blockIdx.x, N.neq, N.nreac));
+  if constexpr (sizeof(T) == 4) tc_setup(&sh.tc);
   for (;;) {
     if (threadIdx.x == 0) sh.ms.model = atomicAdd(counter, 1);
     __syncthreads();
@@ -322,6 +325,7 @@ __global__ void __launch_bounds__(NT, 1) k_solve_models(DevNet N, const ucl_mode
     if (mi >= nmodels) break;
     run_model<T>(C, params, start, mi, max_rows, phys_out, abund_out, nrows_out, flag_out, stats);
   }
+  if constexpr (sizeof(T) == 4) tc_teardown(&sh.tc);
 }
 
 // Batched dense LU (ucl_lu_factor_device): one CTA per matrix, the same
@@ -331,11 +335,15 @@ __global__ void __launch_bounds__(NT) k_lu_batch(T* mats, int n, int* perm, int*
   extern __shared__ __align__(16) char smem[];
   __shared__ int si[LU_SI_INTS];
   __shared__ int lperm[MAX_NEQ];
+  __shared__ TcState tc;
   const int s = blockIdx.x;
   if (s >= nsys) return;
+  const bool use_tc = LuSmem<T>::tc_ok(n);
+  if (use_tc) tc_setup(&tc);
   const int r = block_lu<T>(mats + (size_t)s * n * n, n, perm + (size_t)s * n, smem, si,
-                            scr + (size_t)s * 2 * LuCfg<T>::NB * n, lperm);
+                            scr + (size_t)s * 2 * LuCfg<T>::NB * n, lperm, use_tc ? &tc : nullptr);
   if (threadIdx.x == 0) info[s] = r;
+  if (use_tc) tc_teardown(&tc);
 }
 
 // Rates for a batch of systems (ucl_rates_batch): one CTA per system.
@@ -395,7 +403,7 @@ __global__ void __launch_bounds__(NT) k_rhs_jac(DevNet N, const ucl_model_params
   double* out = y + n;
   double* flux = out + n;
   double* part = flux + N.nreac;
-  double* dfa = part + N.nchunk;
+  double* dfa = part + N.npart;
   double* dfb = dfa + N.nreac;
   double* vec = dfb + N.nreac;
   for (int i = threadIdx.x; i < n; i += NT) y[i] = yin[(size_t)s * n + i];
@@ -411,7 +419,8 @@ __global__ void __launch_bounds__(NT) k_rhs_jac(DevNet N, const ucl_model_params
   if (ydot)
     for (int i = threadIdx.x; i < n; i += NT) ydot[(size_t)s * n + i] = out[i];
   if (jac)
-    dev_jac<false, double>(N, sh.P, sh.S, y, r, nullptr, nullptr, jac + (size_t)s * n * n, flux, dfa, dfb, vec, sh.R);
+    dev_jac<false, double>(N, sh.P, sh.S, y, r, nullptr, nullptr, jac + (size_t)s * n * n, flux, dfa, dfb, vec,
+                           part, sh.R);
 }
 
 }  // namespace ucl
