@@ -136,8 +136,10 @@ int ucl_jac_batch(ucl_ctx* ctx, int nsys, const ucl_model_params* params,
 typedef struct ucl_model_stats {
   int64_t nst, nfe, nje, nlu, nni, ncfn, netf; /* DVODE counters, summed   */
   int32_t n_intervals, n_retries;              /* output rows, retry loops  */
-  double solve_ms;                              /* device latency of model  */
+  double solve_ms;                              /* device time of the model */
   double t_rates_ms, t_rhs_ms, t_jac_ms, t_lu_ms, t_solve_ms; /* phase split  */
+  double queue_ms;   /* arrival (or launch) to start of integration          */
+  double latency_ms; /* arrival (or launch) to completion                    */
 } ucl_model_stats;
 
 /* Integrate whole CLOUD models on the device, one output row per interval
@@ -170,6 +172,18 @@ int ucl_solve_models_device(ucl_ctx* ctx, int nmodels, const ucl_model_params* p
                             double* abund_dev, int* nrows_dev, int* flag_dev,
                             ucl_model_stats* stats_dev, int precision, int max_ctas,
                             void* stream);
+
+/* Serving form of ucl_solve_models_device: request i (params_dev[i], ...)
+ * arrives arrival_s_dev[i] seconds after the launch starts (ascending), is
+ * admitted by the first free slot (slots: as many as fit the context's HBM
+ * budget and the GPU) no earlier than its arrival, and its queue and
+ * latency times are measured from that arrival (stats queue_ms,
+ * latency_ms).  The request queue and the admission live on the device; the
+ * host makes one launch. */
+int ucl_serve_models_device(ucl_ctx* ctx, int nmodels, const ucl_model_params* params_dev,
+                            const double* arrival_s_dev, const double* start_dev, int max_rows,
+                            double* phys_dev, double* abund_dev, int* nrows_dev, int* flag_dev,
+                            ucl_model_stats* stats_dev, int precision, int max_ctas, void* stream);
 
 /* Batched dense LU with partial pivoting of `nsys` row-major n x n matrices
  * in device memory (FP32 for UCL_PREC_MIXED, FP64 otherwise), in place: the

@@ -10,6 +10,8 @@ from uclchem_gb300.params import grid_params, make_param_array
 pytestmark = pytest.mark.gpu
 
 CONFIG1 = {"initialDens": 1e4, "initialTemp": 10.0, "finalTime": 1e6}
+FREEFALL = {"initialDens": 1e2, "initialTemp": 10.0, "finalTime": 5e6, "freefall": True,
+            "endAtFinalDensity": True, "finalDens": 1e5}
 
 
 @pytest.fixture(scope="module")
@@ -49,6 +51,19 @@ def test_grid_points_match_oracle(ctx, oracle, precision):
         assert nrows[k] == onrows[k]
         n = int(nrows[k])
         assert dex_error(ab[k, :n], oab[k, :n]) < 0.01, k
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_freefall_matches_golden(ctx, freefall_golden, precision):
+    """examples/example-output/phase1-full.dat: freefall collapse 1e2 -> 1e5
+    with densdot in the ODE system and the Av update between intervals."""
+    phys, ab, nrows, flags, stats = ctx.solve_models(make_param_array([FREEFALL]), 256, precision=precision)
+    g_phys, g_ab = freefall_golden["phys"], freefall_golden["abund"]
+    n = int(nrows[0])
+    assert flags[0] == 0 and n == len(g_phys)
+    np.testing.assert_allclose(phys[0, :n, 1], g_phys[:, 1], rtol=1e-4)
+    np.testing.assert_allclose(phys[0, :n, 4], g_phys[:, 4], rtol=1e-4)
+    assert dex_error(ab[0, :n], g_ab) < 0.01
 
 
 def test_element_conservation(ctx, net):

@@ -25,13 +25,15 @@ class ModelStats(ctypes.Structure):
                 ("nlu", ctypes.c_int64), ("nni", ctypes.c_int64), ("ncfn", ctypes.c_int64),
                 ("netf", ctypes.c_int64), ("n_intervals", ctypes.c_int32), ("n_retries", ctypes.c_int32),
                 ("solve_ms", ctypes.c_double), ("t_rates_ms", ctypes.c_double), ("t_rhs_ms", ctypes.c_double),
-                ("t_jac_ms", ctypes.c_double), ("t_lu_ms", ctypes.c_double), ("t_solve_ms", ctypes.c_double)]
+                ("t_jac_ms", ctypes.c_double), ("t_lu_ms", ctypes.c_double), ("t_solve_ms", ctypes.c_double),
+                ("queue_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
 
 
 STATS_DTYPE = np.dtype([(n, np.int64) for n in ("nst", "nfe", "nje", "nlu", "nni", "ncfn", "netf")] +
                        [("n_intervals", np.int32), ("n_retries", np.int32), ("solve_ms", np.float64),
                         ("t_rates_ms", np.float64), ("t_rhs_ms", np.float64), ("t_jac_ms", np.float64),
-                        ("t_lu_ms", np.float64), ("t_solve_ms", np.float64)])
+                        ("t_lu_ms", np.float64), ("t_solve_ms", np.float64), ("queue_ms", np.float64),
+                        ("latency_ms", np.float64)])
 assert STATS_DTYPE.itemsize == ctypes.sizeof(ModelStats)
 
 PREC_FP64 = 0
@@ -40,7 +42,7 @@ PREC_MIXED = 1
 EXPORTS = ["ucl_params_default", "ucl_network_load", "ucl_network_free", "ucl_network_nspec",
            "ucl_network_nreac", "ucl_ctx_create", "ucl_ctx_destroy", "ucl_rates_batch", "ucl_rhs_batch",
            "ucl_jac_batch", "ucl_solve_models", "ucl_solve_models_device", "ucl_ctx_slots",
-           "ucl_lu_factor_device"]
+           "ucl_lu_factor_device", "ucl_serve_models_device"]
 
 _LOCK = threading.Lock()
 _LIB = None
@@ -78,6 +80,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
                                                 ctypes.c_int, ctypes.c_int, _vp]
         lib.ucl_ctx_slots.argtypes = [_vp, ctypes.c_int]
         lib.ucl_lu_factor_device.argtypes = [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp]
+        lib.ucl_serve_models_device.argtypes = [_vp, ctypes.c_int, _vp, _vp, _vp, ctypes.c_int, _vp, _vp, _vp, _vp,
+                                                _vp, ctypes.c_int, ctypes.c_int, _vp]
         _LIB = lib
         return lib
 
@@ -173,6 +177,12 @@ class Context:
     def lu_factor_device(self, nsys, n, precision, mats_ptr, perm_ptr, info_ptr, stream=0):
         check(self.lib.ucl_lu_factor_device(self.ctx, nsys, n, precision, mats_ptr, perm_ptr, info_ptr, stream),
               "ucl_lu_factor_device")
+
+    def serve_models_device(self, n, params_ptr, arrival_ptr, start_ptr, max_rows, phys_ptr, abund_ptr, nrows_ptr,
+                            flags_ptr, stats_ptr, precision, max_ctas=0, stream=0):
+        check(self.lib.ucl_serve_models_device(self.ctx, n, params_ptr, arrival_ptr, start_ptr, max_rows, phys_ptr,
+                                               abund_ptr, nrows_ptr, flags_ptr, stats_ptr, precision, max_ctas,
+                                               stream), "ucl_serve_models_device")
 
     def solve_models_device(self, n, params_ptr, start_ptr, max_rows, phys_ptr, abund_ptr, nrows_ptr, flags_ptr,
                             stats_ptr, precision, max_ctas=0, stream=0):

@@ -36,6 +36,7 @@ struct ModelState {
   int flag, row, loop, fail_count, retries, model, go;
   long long nst, nfe, nje, nlu, nni, ncfn, netf;
   unsigned long long t0, tp;
+  unsigned long long ta;       // arrival time of the request (globaltimer ns)
   unsigned long long tacc[5];  // ns in rates, rhs, jac, lu, solve
 };
 

@@ -761,7 +761,7 @@ static int cuda_status(cudaError_t e) { return e == cudaSuccess ? UCL_OK : UCL_E
 template <typename T>
 static int solve_dev(ucl_ctx* c, int nmodels, const ucl_model_params* params_d, const double* start_d,
                      int max_rows, double* phys_d, double* abund_d, int* nrows_d, int* flags_d,
-                     ucl_model_stats* stats_d, int nslots_req) {
+                     ucl_model_stats* stats_d, int nslots_req, const double* arrival_d = nullptr) {
   const int n = c->neq;
   int nslots = sizeof(T) == 4 ? c->slots_fp32 : c->slots_fp64;
   if (nslots_req > 0) nslots = std::min(nslots, nslots_req);
@@ -775,7 +775,7 @@ static int solve_dev(ucl_ctx* c, int nmodels, const ucl_model_params* params_d, 
                j_b = a256((size_t)nslots * n * n * sizeof(T)), perm_b = a256((size_t)nslots * n * 4),
                scr_b = a256((size_t)nslots * 2 * LuCfg<T>::NB * n * sizeof(T)),
                dinv_b = a256((size_t)nslots * dinv_elems(n) * sizeof(T));
-  int rc = c->ws.ensure(yh_b + rate_b + 2 * j_b + perm_b + scr_b + dinv_b + 256);
+  int rc = c->ws.ensure(yh_b + rate_b + 2 * j_b + perm_b + scr_b + dinv_b + 512);
   if (rc) return rc;
   char* base = (char*)c->ws.p;
   SlotArrays<T> A;
@@ -787,10 +787,12 @@ static int solve_dev(ucl_ctx* c, int nmodels, const ucl_model_params* params_d, 
   A.scr = (T*)(base + yh_b + rate_b + 2 * j_b + perm_b);
   A.dinv = (T*)(base + yh_b + rate_b + 2 * j_b + perm_b + scr_b);
   int* counter = (int*)(base + yh_b + rate_b + 2 * j_b + perm_b + scr_b + dinv_b);
-  if (cudaMemsetAsync(counter, 0, sizeof(int), c->stream) != cudaSuccess) return UCL_E_CUDA;
+  unsigned long long* epoch = (unsigned long long*)((char*)counter + 16);
+  if (cudaMemsetAsync(counter, 0, 32, c->stream) != cudaSuccess) return UCL_E_CUDA;
   const SmemLayout L = smem_layout<T>(n, c->nreac, c->tab.nchunk);
   k_solve_models<T><<<nslots, NT, L.total, c->stream>>>(c->tab.dn, params_d, start_d, nmodels, max_rows, phys_d,
-                                                       abund_d, nrows_d, flags_d, stats_d, A, counter);
+                                                       abund_d, nrows_d, flags_d, stats_d, A, counter,
+                                                       epoch, arrival_d);
   return cuda_status(cudaGetLastError());
 }
 
@@ -940,6 +942,27 @@ extern "C" int ucl_jac_batch(ucl_ctx* c, int nsys, const ucl_model_params* param
   if (!c || nsys < 0 || !params || !y || !rates || !av || !jac) return UCL_E_ARG;
   if (nsys == 0) return UCL_OK;
   return rhs_jac(c, nsys, params, y, rates, av, nullptr, jac);
+}
+
+extern "C" int ucl_serve_models_device(ucl_ctx* c, int nmodels, const ucl_model_params* params_d,
+                                       const double* arrival_d, const double* start_d, int max_rows, double* phys_d,
+                                       double* abund_d, int* nrows_d, int* flags_d, ucl_model_stats* stats_d,
+                                       int precision, int max_ctas, void* stream) {
+  if (!c || nmodels < 0 || max_rows < 1 || !params_d || !arrival_d || !phys_d || !abund_d || !nrows_d || !flags_d)
+    return UCL_E_ARG;
+  if (precision != UCL_PREC_FP64 && precision != UCL_PREC_MIXED) return UCL_E_ARG;
+  if (nmodels == 0) return UCL_OK;
+  cudaSetDevice(c->device);
+  cudaStream_t user = (cudaStream_t)stream;
+  cudaStream_t keep = c->stream;
+  if (user) c->stream = user;
+  const int rc = precision == UCL_PREC_MIXED
+                     ? solve_dev<float>(c, nmodels, params_d, start_d, max_rows, phys_d, abund_d, nrows_d, flags_d,
+                                        stats_d, max_ctas, arrival_d)
+                     : solve_dev<double>(c, nmodels, params_d, start_d, max_rows, phys_d, abund_d, nrows_d, flags_d,
+                                         stats_d, max_ctas, arrival_d);
+  c->stream = keep;
+  return rc;
 }
 
 // batched LU of row-major n x n matrices already on the device

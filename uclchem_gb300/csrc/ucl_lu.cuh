@@ -101,9 +101,9 @@ struct LuSmem {
   // (the diagonal-block inversion after the factorisation reuses the area
   // for NWARP staged 32 x 33 tiles)
   __host__ __device__ static constexpr size_t tiles() { return (size_t)NWARP * 32 * 33 * sizeof(T); }
+  __host__ __device__ static constexpr size_t maps_bytes(int n) { return al((size_t)(2 * n + NB) * sizeof(int)); }
   __host__ __device__ static constexpr size_t bytes(int n) {
-    return maps(n) + al((size_t)2 * n * sizeof(int)) + 16 > tiles() ? maps(n) + al((size_t)2 * n * sizeof(int)) + 16
-                                                                     : tiles();
+    return maps(n) + maps_bytes(n) + 16 > tiles() ? maps(n) + maps_bytes(n) + 16 : tiles();
   }
 };
 
@@ -112,6 +112,10 @@ template <typename T>
 __host__ __device__ constexpr size_t lu_smem_bytes(int n) {
   return LuSmem<T>::bytes(n);
 }
+
+// correctly rounded reciprocal (the same value as 1 / x)
+__device__ __forceinline__ float recip_rn(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double recip_rn(double x) { return __drcp_rn(x); }
 
 // |v| as an unsigned key whose integer order is the order of |v|
 __device__ __forceinline__ unsigned long long abs_key(double v) {
@@ -131,12 +135,13 @@ __device__ __forceinline__ unsigned long long warp_max_key(unsigned long long k)
 
 // Factor the m x nb panel at (k0, k0) with partial pivoting, rows held in
 // registers: thread t owns panel rows t + NT*s (s < RPT).  Rows are not
-// moved while the panel is factored; row_at/pos_of record which row sits at
-// each position after the LINPACK-order interchanges (DGEFA's ipvt).  One
-// barrier per column: every warp publishes its best candidate (|v| key, row,
-// and the row's values) in a double-buffered slot, then every warp reduces
-// the NWARP candidates itself.  Ties go to the lowest lane / warp.  Zero
-// pivot: as DGEFA, no interchange and no elimination, info = column + 1.
+// moved while the panel is factored; the pivot row of each column is
+// recorded and, after the panel, row_at/pos_of are built from the
+// LINPACK-order interchanges (DGEFA's ipvt).  One barrier per column: every
+// warp publishes its best candidate (|v| key, row, and the row's values) in
+// a double-buffered slot, then every warp reduces the NWARP candidates
+// itself.  Ties go to the lowest lane / warp.  Zero pivot: no elimination,
+// info = column + 1.
 // Rows are written back to A (panel columns, final positions) and to the
 // shared panel sp for the U12 solve and the trailing update.
 template <typename T, int RPT>
@@ -150,6 +155,7 @@ __device__ __forceinline__ int panel_factor(T* __restrict__ A, int n, int k0, in
   unsigned* ckey = (unsigned*)(smem + LuSmem<T>::ckey(n));  // [2][NWARP][4]
   int* row_at = (int*)(smem + LuSmem<T>::maps(n));
   int* pos_of = row_at + n;
+  int* piv = pos_of + n;  // [NB] pivot row chosen for each column
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const bool vec = (n % W) == 0;
   T a[RPT][NB];
@@ -182,7 +188,8 @@ __device__ __forceinline__ int panel_factor(T* __restrict__ A, int n, int k0, in
       int bs = 0;
 #pragma unroll
       for (int s = 0; s < RPT; ++s) {
-        const unsigned long long k = done[s] ? 0ull : abs_key(a[s][c]);
+        // live rows key |v| + 1 (order kept), finished rows 0
+        const unsigned long long k = done[s] ? 0ull : abs_key(a[s][c]) + 1ull;
         if (k > bk) { bk = k; bs = s; }
       }
       const unsigned long long wk = warp_max_key<T>(bk);
@@ -190,12 +197,18 @@ __device__ __forceinline__ int panel_factor(T* __restrict__ A, int n, int k0, in
       if (lane == owner) {
         T* dst = crow + (size_t)(buf * NWARP + warp) * NB;
 #pragma unroll
-        for (int j = c; j < NB; ++j) {
-          T v = a[0][j];
+        for (int j = (c / W) * W; j < NB; j += W) {
+          V v;
+          T* e = reinterpret_cast<T*>(&v);
 #pragma unroll
-          for (int s = 1; s < RPT; ++s)
-            if (bs == s) v = a[s][j];
-          dst[j] = v;
+          for (int w = 0; w < W; ++w) {
+            T x = a[0][j + w];
+#pragma unroll
+            for (int s = 1; s < RPT; ++s)
+              if (bs == s) x = a[s][j + w];
+            e[w] = x;
+          }
+          *reinterpret_cast<V*>(dst + j) = v;
         }
         unsigned* kk = ckey + (buf * NWARP + warp) * 4;
         kk[0] = (unsigned)wk;
@@ -213,10 +226,12 @@ __device__ __forceinline__ int panel_factor(T* __restrict__ A, int n, int k0, in
       }
       const unsigned long long mk = warp_max_key<T>(ck);
       const int ww = __ffs(__ballot_sync(0xffffffffu, lane < NWARP && ck == mk)) - 1;
-      int pi = __shfl_sync(0xffffffffu, crow_i, ww);
-      if (mk == 0ull) {
-        // zero pivot column: the row at position c stays, nothing eliminated
-        pi = row_at[c];
+      const int pi = __shfl_sync(0xffffffffu, crow_i, ww);
+      if (tid == 0) piv[c] = pi;
+      if (mk == 1ull) {
+        // zero pivot column: nothing is eliminated (DGEFA).  A zero row
+        // other than the one at position c may be taken as the pivot row;
+        // the factors of a singular matrix are not used (info != 0).
         if (info == 0) info = k0 + c + 1;
 #pragma unroll
         for (int s = 0; s < RPT; ++s)
@@ -234,7 +249,7 @@ __device__ __forceinline__ int panel_factor(T* __restrict__ A, int n, int k0, in
             for (int w = 0; w < W; ++w) prow[j + w] = e[w];
           }
         }
-        const T inv = (T)1 / prow[c];
+        const T inv = recip_rn(prow[c]);
 #pragma unroll
         for (int s = 0; s < RPT; ++s) {
           if (done[s]) continue;
@@ -245,13 +260,18 @@ __device__ __forceinline__ int panel_factor(T* __restrict__ A, int n, int k0, in
           for (int j = c + 1; j < NB; ++j) a[s][j] -= l * prow[j];
         }
       }
-      if (tid == 0) {
-        const int q = pos_of[pi], r2 = row_at[c];
-        row_at[c] = pi;
-        row_at[q] = r2;
-        pos_of[pi] = c;
-        pos_of[r2] = q;
-      }
+    }
+  }
+  __syncthreads();
+  // the interchanges of the panel in LINPACK order: position maps
+  if (tid == 0) {
+    for (int c = 0; c < nb; ++c) {
+      const int pi = piv[c];
+      const int q = pos_of[pi], r2 = row_at[c];
+      row_at[c] = pi;
+      row_at[q] = r2;
+      pos_of[pi] = c;
+      pos_of[r2] = q;
     }
   }
   __syncthreads();
@@ -339,14 +359,37 @@ __device__ int block_lu(T* __restrict__ A, int n, int* __restrict__ perm_out, ch
       const int m2 = s_i[39];
       const bool vec = (n % W) == 0;
       for (int pass = 0; pass < 2; ++pass) {
-        for (int q = warp; q < m2; q += NWARP) {
-          const T* src = pass == 0 ? A + (size_t)mv[2 * q + 1] * n : scr + (size_t)q * n;
-          T* dst = pass == 0 ? scr + (size_t)q * n : A + (size_t)mv[2 * q] * n;
-          if (vec) {
-            for (int j = lane * W; j < n; j += 32 * W)
-              if (j < k0 || j >= k0 + nb)
-                *reinterpret_cast<V*>(dst + j) = *reinterpret_cast<const V*>(src + j);
-          } else {
+        if (vec) {
+          // 4 rows per warp at a time, all loads issued before the stores
+          constexpr int RU = 4, CU = 3;
+          for (int q0 = warp * RU; q0 < m2; q0 += NWARP * RU)
+            for (int jb = 0; jb < n; jb += 32 * W * CU) {
+              V v[RU][CU];
+#pragma unroll
+              for (int u = 0; u < RU; ++u) {
+                const int q = q0 + u;
+                const T* src = q < m2 ? (pass == 0 ? A + (size_t)mv[2 * q + 1] * n : scr + (size_t)q * n) : A;
+#pragma unroll
+                for (int t = 0; t < CU; ++t) {
+                  const int j = jb + (lane + 32 * t) * W;
+                  if (q < m2 && j < n && (j < k0 || j >= k0 + nb)) v[u][t] = *reinterpret_cast<const V*>(src + j);
+                }
+              }
+#pragma unroll
+              for (int u = 0; u < RU; ++u) {
+                const int q = q0 + u;
+                T* dst = q < m2 ? (pass == 0 ? scr + (size_t)q * n : A + (size_t)mv[2 * q] * n) : A;
+#pragma unroll
+                for (int t = 0; t < CU; ++t) {
+                  const int j = jb + (lane + 32 * t) * W;
+                  if (q < m2 && j < n && (j < k0 || j >= k0 + nb)) *reinterpret_cast<V*>(dst + j) = v[u][t];
+                }
+              }
+            }
+        } else {
+          for (int q = warp; q < m2; q += NWARP) {
+            const T* src = pass == 0 ? A + (size_t)mv[2 * q + 1] * n : scr + (size_t)q * n;
+            T* dst = pass == 0 ? scr + (size_t)q * n : A + (size_t)mv[2 * q] * n;
             for (int j = lane; j < n; j += 32)
               if (j < k0 || j >= k0 + nb) dst[j] = src[j];
           }
@@ -362,10 +405,15 @@ __device__ int block_lu(T* __restrict__ A, int n, int* __restrict__ perm_out, ch
       // U12 = L11^-1 A12
       for (int jj = tid; jj < ncols; jj += NT) {
         T x[NB];
+        // the whole column of A12 first (independent loads), then the
+        // forward substitution with L11 from shared memory
 #pragma unroll
-        for (int q = 0; q < NB; ++q) {
+        for (int q = 0; q < NB; ++q) x[q] = q < nb ? A[(size_t)(k0 + q) * n + k0 + nb + jj] : (T)0;
+#pragma unroll
+        for (int q = 1; q < NB; ++q) {
           if (q < nb) {
-            T v = A[(size_t)(k0 + q) * n + k0 + nb + jj];
+            T v = x[q];
+#pragma unroll
             for (int p = 0; p < q; ++p) v -= sp[q * LDP + p] * x[p];
             x[q] = v;
           }

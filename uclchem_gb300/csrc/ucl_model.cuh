@@ -228,6 +228,9 @@ __device__ void run_model(Ctx<T>& C, const ucl_model_params* params, const doubl
       st.t_jac_ms = ms.tacc[PH_JAC] * 1e-6;
       st.t_lu_ms = ms.tacc[PH_LU] * 1e-6;
       st.t_solve_ms = ms.tacc[PH_SOLVE] * 1e-6;
+      const unsigned long long t1 = globaltimer_ns();
+      st.queue_ms = ms.t0 > ms.ta ? (double)(ms.t0 - ms.ta) * 1e-6 : 0.0;
+      st.latency_ms = t1 > ms.ta ? (double)(t1 - ms.ta) * 1e-6 : 0.0;
       stats[mi] = st;
     }
   }
@@ -304,12 +307,20 @@ __device__ __forceinline__ Slot<T> slot_of(const SlotArrays<T>& A, int s, int n,
   return W;
 }
 
-// Persistent solver: each CTA pulls model indices from a device counter.
+// bounded wait of the admission loop: at most this many sleeps of 20 us
+constexpr unsigned ADMIT_SLEEP_LIMIT = 1u << 26;
+
+// Persistent solver: each CTA pulls model indices from a device counter
+// (requests in index order).  The launch epoch is the first CTA's start
+// time.  With an arrival schedule (seconds after the epoch, ascending), a
+// request is not started before its arrival; queue and latency times are
+// measured from arrival (from the epoch without a schedule).
 template <typename T>
 __global__ void __launch_bounds__(NT, 1) k_solve_models(DevNet N, const ucl_model_params* params, const double* start,
                                                      int nmodels, int max_rows, double* phys_out, double* abund_out,
                                                      int* nrows_out, int* flag_out, ucl_model_stats* stats,
-                                                     SlotArrays<T> ws, int* counter) {
+                                                     SlotArrays<T> ws, int* counter, unsigned long long* epoch,
+                                                     const double* arrival_s) {
   extern __shared__ __align__(16) char smem[];
   __shared__ Shared sh;
   __shared__ DevNet sN;
@@ -318,8 +329,24 @@ __global__ void __launch_bounds__(NT, 1) k_solve_models(DevNet N, const ucl_mode
   __syncthreads();
   Ctx<T> C = make_ctx<T>(&sN, &sh, smem, L, slot_of(ws, blockIdx.x, N.neq, N.nreac));
   if constexpr (sizeof(T) == 4) tc_setup(&sh.tc);
+  __shared__ unsigned long long t_epoch;
+  if (threadIdx.x == 0) {
+    const unsigned long long now = globaltimer_ns();
+    const unsigned long long old = atomicCAS(epoch, 0ull, now);
+    t_epoch = old ? old : now;
+  }
   for (;;) {
-    if (threadIdx.x == 0) sh.ms.model = atomicAdd(counter, 1);
+    if (threadIdx.x == 0) {
+      sh.ms.model = atomicAdd(counter, 1);
+      const int mi = sh.ms.model;
+      sh.ms.ta = t_epoch;
+      if (mi < nmodels && arrival_s) {
+        const double a = arrival_s[mi];
+        const unsigned long long ta = t_epoch + (a > 0.0 ? (unsigned long long)(a * 1e9) : 0ull);
+        sh.ms.ta = ta;
+        for (unsigned it = 0; it < ADMIT_SLEEP_LIMIT && globaltimer_ns() < ta; ++it) __nanosleep(20000);
+      }
+    }
     __syncthreads();
     const int mi = sh.ms.model;
     if (mi >= nmodels) break;

@@ -109,17 +109,15 @@ __device__ __forceinline__ void tc_commit(unsigned long long* mbar) {
                : "memory");
 }
 // 32 lanes x 8 consecutive columns of TMEM -> 8 registers per thread
-__device__ __forceinline__ void tc_ld8(unsigned taddr, float* v) {
-  unsigned r[8];
+// (issue only; the values are valid after tc_ld_wait)
+__device__ __forceinline__ void tc_ld8(unsigned taddr, unsigned* r) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
       : "r"(taddr)
       : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
+__device__ __forceinline__ void tc_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // CTA prologue / epilogue of kernels that use the tensor cores: TMEM
 // allocation by warp 0, mbarrier set-up by thread 0.  All threads call.
@@ -216,6 +214,32 @@ __device__ bool tc_trailing_update(float* __restrict__ A, int n, int r0g, int c0
       }
       tc_commit(&tc->mbar);
     }
+    // epilogue: warp w reads TMEM lanes 32*(w%4).. (its sub-partition),
+    // columns of half w/4, and updates its row of A22 in chunks of 32
+    // columns; the row segment of each chunk is loaded before it is needed
+    // (the first one while the MMAs run)
+    const int q = warp & 3, half = warp >> 2;
+    const int cw = np / 2;  // multiple of 8
+    const int row = m0 + q * 32 + lane;
+    const bool live = row < R;
+    const bool vec = ((n & 3) == 0) && ((c0g & 3) == 0);
+    float* dst = A + (size_t)(r0g + (live ? row : 0)) * n + c0g;
+    const int cbeg = half * cw, cend = (half + 1) * cw;
+    float cv[32];
+    auto load_chunk = [&](int c) {
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int cc = c + 4 * u;
+        if (live && cc < cend && cc + 4 <= nc && vec) {
+          const float4 x = *reinterpret_cast<const float4*>(dst + cc);
+          cv[4 * u] = x.x; cv[4 * u + 1] = x.y; cv[4 * u + 2] = x.z; cv[4 * u + 3] = x.w;
+        } else {
+#pragma unroll
+          for (int i = 0; i < 4; ++i) cv[4 * u + i] = (live && cc < cend && cc + i < nc) ? dst[cc + i] : 0.f;
+        }
+      }
+    };
+    load_chunk(cbeg);
     const bool done = mbar_wait(&tc->mbar, tc->phase);
     tc_fence_after();
     if (!done) {
@@ -224,27 +248,33 @@ __device__ bool tc_trailing_update(float* __restrict__ A, int n, int r0g, int c0
       ok = false;
       if (tid == 0) tc->err = 1;
     } else {
-      // epilogue: warp w reads TMEM lanes 32*(w%4).. (its sub-partition),
-      // columns of half w/4, and updates its rows of A22
-      const int q = warp & 3, half = warp >> 2;
-      const int cw = np / 2;  // multiple of 8
-      const int row = m0 + q * 32 + lane;
-      float* dst = A + (size_t)(r0g + row) * n + c0g;
-      for (int c = half * cw; c < (half + 1) * cw; c += 8) {
-        float v[8];
-        tc_ld8(tc->tmem + ((unsigned)(q * 32) << 16) + (unsigned)c, v);
-        if (row < R) {
-          if (c + 8 <= nc && ((n & 3) == 0) && ((c0g & 3) == 0)) {
-            float4 x0 = *reinterpret_cast<float4*>(dst + c);
-            float4 x1 = *reinterpret_cast<float4*>(dst + c + 4);
-            x0.x -= v[0]; x0.y -= v[1]; x0.z -= v[2]; x0.w -= v[3];
-            x1.x -= v[4]; x1.y -= v[5]; x1.z -= v[6]; x1.w -= v[7];
-            *reinterpret_cast<float4*>(dst + c) = x0;
-            *reinterpret_cast<float4*>(dst + c + 4) = x1;
-          } else {
+      for (int c = cbeg; c < cend; c += 32) {
+        unsigned d[32];
 #pragma unroll
-            for (int i = 0; i < 8; ++i)
-              if (c + i < nc) dst[c + i] -= v[i];
+        for (int u = 0; u < 4; ++u) {
+          if (c + 8 * u < cend) tc_ld8(tc->tmem + ((unsigned)(q * 32) << 16) + (unsigned)(c + 8 * u), d + 8 * u);
+          else {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) d[8 * u + i] = 0u;
+          }
+        }
+        tc_ld_wait();
+        float out[32];
+#pragma unroll
+        for (int i = 0; i < 32; ++i) out[i] = cv[i] - __uint_as_float(d[i]);
+        if (c + 32 < cend) load_chunk(c + 32);
+        if (live) {
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int cc = c + 4 * u;
+            if (cc < cend && cc + 4 <= nc && vec) {
+              *reinterpret_cast<float4*>(dst + cc) =
+                  make_float4(out[4 * u], out[4 * u + 1], out[4 * u + 2], out[4 * u + 3]);
+            } else {
+#pragma unroll
+              for (int i = 0; i < 4; ++i)
+                if (cc < cend && cc + i < nc) dst[cc + i] = out[4 * u + i];
+            }
           }
         }
       }
