@@ -194,6 +194,30 @@ int ucl_serve_models_device(ucl_ctx* ctx, int nmodels, const ucl_model_params* p
 int ucl_lu_factor_device(ucl_ctx* ctx, int nsys, int n, int precision, void* mats_dev,
                          int* perm_dev, int* info_dev, void* stream);
 
+/* Size of the fixed device scratch of ucl_lu_factor_device_static. */
+#define UCL_LU_STATIC_SCRATCH_BYTES (16u << 20)
+
+/* The batched LU of ucl_lu_factor_device without a context and without
+ * allocating anything: no cudaMalloc/cudaFree and no allocating library
+ * call, for callers whose device memory is all owned by another allocator
+ * (a framework's caching allocator, or a serving loop that has handed its
+ * whole HBM budget to resident model state) and callers that must not pay
+ * the implicit device synchronisation of an allocation.  This entry point
+ * has no counterpart in the reference (DGEFA works in the caller's arrays).
+ * The row-interchange scratch is a fixed static device array of
+ * UCL_LU_STATIC_SCRATCH_BYTES shared by every call; at most
+ * UCL_LU_STATIC_SCRATCH_BYTES / (2 * NB * n * sizeof(element)) matrices are
+ * in flight at once (NB = 32 FP32, 16 FP64), the rest are taken in turn by
+ * the same CTAs.  Nothing in the scratch has to start at zero.  Calls that
+ * overlap in time (different streams, or different host threads without
+ * ordering) race on the scratch and must not be issued.  The first call on
+ * each device performs the one-time set-up on that device (the scratch's
+ * device address and the kernels' shared-memory limits), so make that first
+ * call before any stream capture.  Uses the current device; arguments as in
+ * ucl_lu_factor_device; n > 520 or n % 4 != 0 is rejected with UCL_E_ARG. */
+int ucl_lu_factor_device_static(int nsys, int n, int precision, void* mats_dev, int* perm_dev,
+                                int* info_dev, void* stream);
+
 /* Models the context integrates concurrently at the given precision. */
 int ucl_ctx_slots(const ucl_ctx* ctx, int precision);
 

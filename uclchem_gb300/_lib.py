@@ -42,7 +42,7 @@ PREC_MIXED = 1
 EXPORTS = ["ucl_params_default", "ucl_network_load", "ucl_network_free", "ucl_network_nspec",
            "ucl_network_nreac", "ucl_ctx_create", "ucl_ctx_destroy", "ucl_rates_batch", "ucl_rhs_batch",
            "ucl_jac_batch", "ucl_solve_models", "ucl_solve_models_device", "ucl_ctx_slots",
-           "ucl_lu_factor_device", "ucl_serve_models_device"]
+           "ucl_lu_factor_device", "ucl_serve_models_device", "ucl_lu_factor_device_static"]
 
 _LOCK = threading.Lock()
 _LIB = None
@@ -80,6 +80,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
                                                 ctypes.c_int, ctypes.c_int, _vp]
         lib.ucl_ctx_slots.argtypes = [_vp, ctypes.c_int]
         lib.ucl_lu_factor_device.argtypes = [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp]
+        lib.ucl_lu_factor_device_static.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp]
         lib.ucl_serve_models_device.argtypes = [_vp, ctypes.c_int, _vp, _vp, _vp, ctypes.c_int, _vp, _vp, _vp, _vp,
                                                 _vp, ctypes.c_int, ctypes.c_int, _vp]
         _LIB = lib

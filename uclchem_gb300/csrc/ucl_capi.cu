@@ -8,6 +8,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <utility>
 #include <vector>
@@ -988,6 +989,60 @@ extern "C" int ucl_lu_factor_device(ucl_ctx* c, int nsys, int n, int precision, 
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
   return precision == UCL_PREC_MIXED ? lu_dev<float>(c, nsys, n, mats_dev, perm_dev, info_dev, st)
                                      : lu_dev<double>(c, nsys, n, mats_dev, perm_dev, info_dev, st);
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free batched LU.  The row-interchange scratch lives in a fixed
+// file-scope device array; the kernel's grid is capped so that every CTA has
+// its own part of it.  Set-up (symbol address, shared-memory attributes) is
+// done once per device by the first call on that device.
+static __device__ __align__(256) unsigned char g_lu_scratch[UCL_LU_STATIC_SCRATCH_BYTES];
+
+namespace {
+struct StaticLuDev {
+  std::once_flag once;
+  int rc = UCL_E_CUDA;
+  void* scratch = nullptr;
+};
+StaticLuDev g_static_lu[64];
+}  // namespace
+
+template <typename T>
+static int lu_static(int nsys, int n, void* mats, int* perm, int* info, void* scratch, cudaStream_t st) {
+  const size_t per = (size_t)2 * LuCfg<T>::NB * n * sizeof(T);
+  const int cap = (int)(UCL_LU_STATIC_SCRATCH_BYTES / per);
+  if (cap < 1) return UCL_E_ARG;
+  const int grid = std::min(nsys, cap);
+  k_lu_batch_strided<T><<<grid, NT, lu_smem_bytes<T>(n), st>>>((T*)mats, n, perm, info, (T*)scratch, nsys);
+  return cuda_status(cudaGetLastError());
+}
+
+extern "C" int ucl_lu_factor_device_static(int nsys, int n, int precision, void* mats_dev, int* perm_dev,
+                                           int* info_dev, void* stream) {
+  if (nsys < 0 || n < 2 || n > MAX_NEQ || (n % 4) != 0 || !mats_dev || !perm_dev || !info_dev) return UCL_E_ARG;
+  if (precision != UCL_PREC_FP64 && precision != UCL_PREC_MIXED) return UCL_E_ARG;
+  if (((uintptr_t)mats_dev & 15) != 0) return UCL_E_ARG;
+  if (nsys == 0) return UCL_OK;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return UCL_E_CUDA;
+  StaticLuDev& S = g_static_lu[dev];
+  std::call_once(S.once, [&S]() {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_lu_scratch) != cudaSuccess) return;
+    const int sm32 = (int)std::max(lu_smem_bytes<float>(MAX_NEQ), lu_smem_bytes<float>(TC_MAX_N));
+    const int sm64 = (int)lu_smem_bytes<double>(MAX_NEQ);
+    if (cudaFuncSetAttribute(k_lu_batch_strided<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(k_lu_batch_strided<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm64) !=
+            cudaSuccess)
+      return;
+    S.scratch = p;
+    S.rc = UCL_OK;
+  });
+  if (S.rc != UCL_OK) return S.rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  return precision == UCL_PREC_MIXED ? lu_static<float>(nsys, n, mats_dev, perm_dev, info_dev, S.scratch, st)
+                                     : lu_static<double>(nsys, n, mats_dev, perm_dev, info_dev, S.scratch, st);
 }
 
 // capacity query used by the host front end

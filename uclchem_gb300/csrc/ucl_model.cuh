@@ -373,6 +373,26 @@ __global__ void __launch_bounds__(NT) k_lu_batch(T* mats, int n, int* perm, int*
   if (use_tc) tc_teardown(&tc);
 }
 
+// Batched LU with a grid capped by the scratch it is given: CTA b factors
+// matrices b, b + gridDim.x, ... and uses scratch rows [b * 2*NB*n, ...).
+template <typename T>
+__global__ void __launch_bounds__(NT) k_lu_batch_strided(T* mats, int n, int* perm, int* info, T* scr, int nsys) {
+  extern __shared__ __align__(16) char smem[];
+  __shared__ int si[LU_SI_INTS];
+  __shared__ int lperm[MAX_NEQ];
+  __shared__ TcState tc;
+  const bool use_tc = LuSmem<T>::tc_ok(n);
+  if (use_tc) tc_setup(&tc);
+  T* my_scr = scr + (size_t)blockIdx.x * 2 * LuCfg<T>::NB * n;
+  for (int s = blockIdx.x; s < nsys; s += gridDim.x) {
+    const int r = block_lu<T>(mats + (size_t)s * n * n, n, perm + (size_t)s * n, smem, si, my_scr, lperm,
+                              use_tc ? &tc : nullptr);
+    if (threadIdx.x == 0) info[s] = r;
+    __syncthreads();
+  }
+  if (use_tc) tc_teardown(&tc);
+}
+
 // Rates for a batch of systems (ucl_rates_batch): one CTA per system.
 __global__ void __launch_bounds__(NT) k_rates(DevNet N, const ucl_model_params* params, double* abund,
                                               const double* av, double* phi, double* rates, int nsys) {
