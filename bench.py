@@ -37,6 +37,11 @@ def workload(models: int, final_time: float) -> str:
     return (f"{models}-point static CLOUD grid (seeded), default network (335 species, 3203 reactions), "
             f"{final_time:g} yr, reltol 1e-8")
 MAX_ROWS = 64
+# DRAM bytes (read + write) of the mixed solver per model-step, from one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) of the 152-model,
+# 1e4-yr grid launch: 113.6 GB over 152 x 4094 model-steps.  Traffic scales
+# with model-steps once the slots' working set exceeds L2.
+DRAM_BYTES_PER_MODEL_STEP = 1.83e5
 SEED = 20261203
 
 
@@ -54,6 +59,8 @@ def parse():
     ap.add_argument("--warmup-final-time", type=float, default=1e3, help="finalTime (yr) of warm-up models")
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
     ap.add_argument("--final-time", type=float, default=1e6, help="finalTime (yr) of the grid models")
+    ap.add_argument("--kernel", default="solve", choices=["solve", "lu"],
+                    help="lu: time the batched Newton-matrix LU alone (--models matrices)")
     return ap.parse_args()
 
 
@@ -324,10 +331,22 @@ def our_arm(args):
         "gpu_launches": args.steps,
         "clocks": clocks,
         "counters": {k: float(stats[k].mean()) for k in ("nst", "nfe", "nje", "nlu", "nni")},
+        # device phase timers of the timed step (globaltimer, per call and share of model time)
+        "phase_us_per_call": {
+            "rhs": 1e3 * float(stats["t_rhs_ms"].sum() / max(stats["nfe"].sum(), 1)),
+            "jacobian": 1e3 * float(stats["t_jac_ms"].sum() / max(stats["nje"].sum(), 1)),
+            "lu": 1e3 * float(stats["t_lu_ms"].sum() / max(stats["nlu"].sum(), 1)),
+            "solve": 1e3 * float(stats["t_solve_ms"].sum() / max(stats["nni"].sum(), 1))},
+        "phase_share": {k: float(stats[f"t_{k}_ms"].sum() / max(stats["solve_ms"].sum(), 1e-30))
+                        for k in ("rates", "rhs", "jac", "lu", "solve")},
         "roofline": {"bound": "tensor", "achieved": mat_tflops, "peak": peak, "unit": "TFLOP/s",
-                     "frac": mat_tflops / peak, "traffic": None,
-                     "note": "k_solve_models: counted LU (2/3 n^3) + solve (2 n^2) flops per step / step time; "
-                             "peak = measured dense bf16"},
+                     "frac": mat_tflops / peak,
+                     "traffic": DRAM_BYTES_PER_MODEL_STEP * float(stats["nst"].sum()) / args.steps,
+                     "note": "k_solve_models: LU (2/3 n^3 per factorisation) + triangular solves (2 n^2 per "
+                             "Newton iteration) counted by the device, over the step time, against the measured "
+                             "dense bf16 peak (the LU's trailing update runs on the tensor cores); the kernel is "
+                             "latency-bound (one CTA per model, barrier-separated phases), hence the small "
+                             "fraction; traffic = DRAM bytes per model-step from one ncu capture x model-steps"},
         "cpu_baseline": cpu,
         "wall_s": wall,
     }
@@ -335,9 +354,46 @@ def our_arm(args):
     ctx.close()
 
 
+def lu_kernel(args):
+    """Batched Newton-matrix LU alone (ucl_lu_factor_device): --models
+    matrices of the network's size (I - c*J-like, random), FP32 and FP64,
+    timed with CUDA events; prints one line per precision."""
+    import torch
+    from uclchem_gb300 import _lib, network
+    ctx = _lib.Context(network.DEFAULT_BLOB, device=0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    n, B = ctx.neq, args.models
+    rng = np.random.default_rng(SEED)
+    for prec, dt in ((_lib.PREC_MIXED, torch.float32), (_lib.PREC_FP64, torch.float64)):
+        A = (torch.eye(n, dtype=torch.float64)[None] -
+             torch.from_numpy(rng.standard_normal((B, n, n)) * 10.0 ** rng.uniform(-3, 1, (B, 1, n)))).to(dt).cuda()
+        m = torch.empty_like(A)
+        perm = torch.empty((B, n), dtype=torch.int32, device="cuda")
+        info = torch.empty(B, dtype=torch.int32, device="cuda")
+        ts = []
+        for it in range(args.warmup + args.steps):
+            m.copy_(A)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.lu_factor_device(B, n, prec, m.data_ptr(), perm.data_ptr(), info.data_ptr(), stream.cuda_stream)
+            e1.record(stream)
+            stream.synchronize()
+            if it >= args.warmup:
+                ts.append(e0.elapsed_time(e1))
+        ms = float(np.median(ts))
+        flop = 2.0 / 3.0 * n ** 3 * B
+        print(json.dumps({"kernel": "k_lu_batch", "precision": "fp32" if prec == _lib.PREC_MIXED else "fp64",
+                          "n": n, "matrices": B, "ms": ms, "us_per_matrix_wave": ms * 1e3 / max(1, -(-B // 152)),
+                          "tflops": flop / (ms * 1e-3) / 1e12, "info_max": int(info.max())}), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.kernel == "lu":
+        lu_kernel(args)
+    elif args.impl == "reference":
         reference_arm(args)
     else:
         our_arm(args)

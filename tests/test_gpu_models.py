@@ -86,3 +86,22 @@ def test_failure_codes_from_host_injection(ctx):
     params = make_param_array([CONFIG1])
     phys, ab, nrows, flags, stats = ctx.solve_models(params, 8, precision=1)
     assert flags[0] == -6 and nrows[0] == 8
+
+
+def test_python_api_cloud_mirrors_reference_layout(oracle):
+    """uclchem.model.cloud's calling convention (src/uclchem/model.py:227-316)
+    on the device path: the [flag, abundances...] list, the array tuple, the
+    parameter-error flag and a restart from a previous final abundance."""
+    from uclchem_gb300 import model
+    pd = {"initialDens": 1e4, "initialTemp": 10.0, "finalTime": 1e4}
+    out = model.cloud(pd, out_species=["CO", "H2O"])
+    assert out[0] == 0 and len(out) == 3 and min(out[1:]) > 0
+    phys, chem, rates, start, flag = model.cloud(pd, return_array=True)
+    assert flag == 0 and rates is None
+    assert phys.shape[1:] == (1, 8) and chem.shape[1:] == (1, 335) and start.shape == (335,)
+    ophys, oab, oflag, _ = oracle.cloud(pd, max_rows=64)
+    assert dex_error(chem[:, 0, :], oab) < 0.01
+    assert model.cloud({"notAParameter": 1.0})[0] == -1
+    phys2, chem2, _, _, flag2 = model.cloud({"initialDens": 1e4, "initialTemp": 10.0, "finalTime": 1e3},
+                                             return_array=True, starting_chemistry=start)
+    assert flag2 == 0 and np.allclose(chem2[0, 0, :], start, rtol=1e-6, atol=1e-20)

@@ -27,6 +27,9 @@ struct DvState {
   double h, hscal, hu, hnew, rc, rl1, prl1, tn, eta, etamax, etaq, etaqm1, conp, crate, drc, acnrm;
   double el[14], tq[6], tau[14];
   double del, delp, dsm, told, uround, srur, tolsf;
+  double cs;    // 2/(1+rc) when rc != 1 (corrector scaling), formed once per Newton solve
+  double rtq2;  // 1/tq[2], formed once per accepted step
+  int cs_on;
   int nq, l, lmax, maxord, nqwait, newq, newh, kflag, jstart, jcur, icf, ipup, nslp, nslj;
   int nst, nfe, nje, nlu, nni, ncfn, netf, ncf, m, jok, nls_out, state, istate, ierpj, mxstep;
 };
@@ -48,7 +51,7 @@ struct Shared {
   SysPhys S;
   RhsScal R;
   ucl_model_params P;
-  double red[NWARP + 2];
+  double red[NWARP + 6];  // block sums; [NWARP+1..NWARP+4] scalars of the step control
   int si[LU_SI_INTS];
   int lperm[MAX_NEQ];
   TcState tc;
@@ -181,6 +184,11 @@ __device__ int dv_nlsd(Ctx<T>& C, int nflag) {
       __syncthreads();
       if (d.ierpj) goto fail70;
     }
+    if (tid == 0) {
+      // scalar FP64 once, not in every thread (FP64 issue is costly on this GPU)
+      d.cs_on = fabs(d.rc - 1.0) > 0.0;
+      d.cs = d.cs_on ? 2.0 / (1.0 + d.rc) : 1.0;
+    }
     for (int i = tid; i < n; i += NT) C.acor[i] = 0.0;
     __syncthreads();
     for (;;) {
@@ -195,8 +203,8 @@ __device__ int dv_nlsd(Ctx<T>& C, int nflag) {
       {
         // scale by 2/(1+rc) when rc != 1, weighted norm of the correction,
         // acor += correction, y = yh0 + acor: one pass, one reduction
-        const bool scale = fabs(d.rc - 1.0) > 0.0;
-        const double cs = scale ? 2.0 / (1.0 + d.rc) : 1.0;
+        const bool scale = d.cs_on != 0;
+        const double cs = d.cs;
         double ss = 0.0;
         for (int i = tid; i < n; i += NT) {
           const double yi = scale ? cs * C.y[i] : C.y[i];
@@ -241,31 +249,45 @@ fail70:
   return -1;
 }
 
-// DVSET, BDF coefficients (scalar)
-__device__ void dv_set(DvState& d) {
-  const double flotl = (double)d.l;
-  const int nq = d.nq;
-  double* el = d.el;
-  double* tq = d.tq;
-  for (int i = 3; i <= d.l; i++) el[i] = 0.0;
+// DVSET, BDF coefficients, by warp 0 (all 32 lanes call).  The divisions,
+// which dominate this scalar code (FP64 issue is per warp instruction, and
+// slow), run three at a time in parallel lanes: the partial step ratios
+// h/hsum_j, then the independent quotients of the error constants, then the
+// two that depend on those.  The arithmetic (operands and order) is the
+// sequential DVSET's, so the results are bit-identical to it.  Also forms
+// rl1 = 1/el[2] and rc <- rc * (rl1/prl1), prl1 = rl1 (DVSTEP after DVSET).
+__device__ void dv_set_w(DvState& d) {
+  const int lane = threadIdx.x & 31;
+  const int nq = d.nq, l = d.l;
+  const double flotl = (double)l;
+  const double kR[8] = {0.0, 1.0, 1.0 / 2.0, 1.0 / 3.0, 1.0 / 4.0, 1.0 / 5.0, 1.0 / 6.0, 1.0 / 7.0};
+  // round 1: lane j (1..nq) forms hsum_j = h + tau[1] + ... + tau[j] and h/hsum_j
+  double hs = d.h;
+  for (int j = 1; j <= nq; ++j)
+    if (j <= lane) hs = hs + d.tau[j];
+  const double rxl = d.h / hs;
+  double rx[6];
+#pragma unroll
+  for (int j = 1; j <= 5; ++j) rx[j] = __shfl_sync(0xffffffffu, rxl, j);
+  // the el recurrence (every lane, identical)
+  double el[7];
+  for (int i = 0; i < 7; i++) el[i] = 0.0;
   el[1] = 1.0;
   el[2] = 1.0;
-  double alph0 = -1.0, ahatn0 = -1.0, hsum = d.h, rxi = 1.0, rxis = 1.0;
+  double alph0 = -1.0, ahatn0 = -1.0, rxi = 1.0, rxis = 1.0;
   if (nq != 1) {
     for (int j = 1; j <= nq - 2; j++) {
-      hsum = hsum + d.tau[j];
-      rxi = d.h / hsum;
+      rxi = rx[j];
       const int jp1 = j + 1;
-      alph0 = alph0 - 1.0 / (double)jp1;
+      alph0 = alph0 - kR[jp1];
       for (int ib = 1; ib <= jp1; ib++) {
         const int i = (j + 3) - ib;
         el[i] = el[i] + el[i - 1] * rxi;
       }
     }
-    alph0 = alph0 - 1.0 / (double)nq;
+    alph0 = alph0 - kR[nq];
     rxis = -el[2] - alph0;
-    hsum = hsum + d.tau[nq - 1];
-    rxi = d.h / hsum;
+    rxi = rx[nq - 1];
     ahatn0 = -el[2] - rxi;
     for (int ib = 1; ib <= nq; ib++) {
       const int i = (nq + 2) - ib;
@@ -274,22 +296,46 @@ __device__ void dv_set(DvState& d) {
   }
   const double t1 = 1.0 - ahatn0 + alph0;
   const double t2 = 1.0 + (double)nq * t1;
-  tq[2] = fabs(alph0 * t2 / t1);
-  tq[5] = fabs(t2 / (el[d.l] * rxi / rxis));
-  if (d.nqwait == 1) {
-    const double cnqm1 = rxis / el[d.l];
-    const double t3 = alph0 + 1.0 / (double)nq;
-    const double t4 = ahatn0 + rxi;
-    double elp = t3 / (1.0 - t4 + t3);
-    tq[1] = fabs(elp / cnqm1);
-    hsum = hsum + d.tau[nq];
-    rxi = d.h / hsum;
-    const double t5 = alph0 - 1.0 / (double)(nq + 1);
-    const double t6 = ahatn0 - rxi;
-    elp = t2 / (1.0 - t6 + t5);
-    tq[3] = fabs(elp * rxi * (flotl + 1.0) * t5);
+  const double t3 = alph0 + kR[nq];
+  const double t4 = ahatn0 + rxi;
+  const double rxn = rx[nq];  // h / hsum_nq, for the order-raise constant
+  const double t5 = alph0 - kR[nq + 1];
+  const double t6 = ahatn0 - rxn;
+  // round 2: independent quotients
+  double num, den;
+  switch (lane) {
+    case 0: num = alph0 * t2; den = t1; break;           // tq[2]
+    case 1: num = el[l] * rxi; den = rxis; break;        // then t2 / this: tq[5]
+    case 2: num = rxis; den = el[l]; break;              // cnqm1
+    case 3: num = t3; den = 1.0 - t4 + t3; break;        // elp (tq[1])
+    case 4: num = t2; den = 1.0 - t6 + t5; break;        // elp (tq[3])
+    default: num = 1.0; den = el[2]; break;              // rl1
   }
-  tq[4] = 0.1 * tq[2];
+  const double q2 = num / den;
+  const double q_tq2 = __shfl_sync(0xffffffffu, q2, 0), q_b = __shfl_sync(0xffffffffu, q2, 1);
+  const double q_cnqm1 = __shfl_sync(0xffffffffu, q2, 2), q_elp1 = __shfl_sync(0xffffffffu, q2, 3);
+  const double q_elp2 = __shfl_sync(0xffffffffu, q2, 4), rl1 = __shfl_sync(0xffffffffu, q2, 5);
+  // round 3: the quotients of quotients
+  if (lane == 0) { num = t2; den = q_b; }
+  else if (lane == 1) { num = q_elp1; den = q_cnqm1; }
+  else { num = rl1; den = d.prl1; }
+  const double q3 = num / den;
+  const double q_tq5 = __shfl_sync(0xffffffffu, q3, 0), q_tq1 = __shfl_sync(0xffffffffu, q3, 1);
+  const double q_rc = __shfl_sync(0xffffffffu, q3, 2);
+  if (lane == 0) {
+    for (int i = 1; i <= l; i++) d.el[i] = el[i];
+    d.tq[2] = fabs(q_tq2);
+    d.tq[5] = fabs(q_tq5);
+    if (d.nqwait == 1) {
+      d.tq[1] = fabs(q_tq1);
+      d.tq[3] = fabs(q_elp2 * rxn * (flotl + 1.0) * t5);
+    }
+    d.tq[4] = 0.1 * d.tq[2];
+    d.rl1 = rl1;
+    d.rc = d.rc * q_rc;
+    d.prl1 = rl1;
+  }
+  __syncwarp();
 }
 
 // DVJUST, BDF branch: el by thread 0, then the Nordsieck update by all
@@ -410,12 +456,7 @@ __device__ void dv_step(Ctx<T>& C) {
       for (int jb = 1; jb <= nq; jb++)
         for (int c = nq - jb; c < nq; c++) yh[(size_t)c * n + i] += yh[(size_t)(c + 1) * n + i];
     }
-    if (tid == 0) {
-      dv_set(d);
-      d.rl1 = 1.0 / d.el[2];
-      d.rc = d.rc * (d.rl1 / d.prl1);
-      d.prl1 = d.rl1;
-    }
+    if ((tid >> 5) == 0) dv_set_w(d);
     __syncthreads();
     nflag = dv_nlsd<T>(C, nflag);
     if (nflag != 0) {
@@ -457,6 +498,7 @@ __device__ void dv_step(Ctx<T>& C) {
         d.nqwait--;
         d.state = (!((d.l == d.lmax) || (d.nqwait != 1))) ? 1 : 0;  // save acor for an order increase
         if (d.state) d.conp = d.tq[5];
+        d.rtq2 = 1.0 / d.tq[2];
       }
       __syncthreads();
       if (d.state) {
@@ -470,25 +512,45 @@ __device__ void dv_step(Ctx<T>& C) {
         }
         __syncthreads();
       } else {
-        // L130: order and step selection
-        const double flotl = (double)d.l;
-        if (tid == 0) d.etaq = 1.0 / (pow(BIAS2 * d.dsm, 1.0 / flotl) + ADDON);
+        // L130: order and step selection.  Scalar FP64 (pow) runs in lanes of
+        // warp 0 only: one warp-wide pow for the up-to-three candidates.
+        const int l = d.l;
+        const bool sel = (d.nqwait == 0);
+        const int lane = tid & 31, warp = tid >> 5;
+        double ddn = 0.0, dup = 0.0;
+        if (sel) {
+          if (d.nq != 1) ddn = bnorm(yh + (size_t)(l - 1) * n, C.ewt, n, C.sh->red) / d.tq[1];
+          if (l != d.lmax) {
+            if (tid == 0) C.sh->red[NWARP + 1] = (d.tq[5] / d.conp) * pow(d.h / d.tau[2], (double)l);
+            __syncthreads();
+            const double cnquot = C.sh->red[NWARP + 1];
+            for (int i = tid; i < n; i += NT) C.savf[i] = C.acor[i] - cnquot * yh[(size_t)(d.lmax - 1) * n + i];
+            dup = bnorm(C.savf, C.ewt, n, C.sh->red) / d.tq[3];
+          }
+        }
+        if (warp == 0) {
+          // lane 0: eta for the same order (etaq); lanes 1, 2: order q-1, q+1
+          const double x = BIAS2 * d.dsm;
+          // without an order decision, etaq only matters when it reaches
+          // THRESH: (BIAS2*dsm)^(1/l) > 1/THRESH - ADDON means it does not
+          // (the margin keeps pow's rounding out of the decision)
+          double cthr = 1.0 / THRESH - ADDON, thr = cthr;
+          for (int k = 1; k < l; ++k) thr *= cthr;
+          const bool need_q = sel || !(x > thr * (1.0 + 1e-9));
+          const bool need_m = sel && d.nq != 1, need_p = sel && l != d.lmax;
+          const bool need = (lane == 0 && need_q) || (lane == 1 && need_m) || (lane == 2 && need_p);
+          const double base = lane == 0 ? x : lane == 1 ? BIAS1 * ddn : BIAS3 * dup;
+          const double ex = lane == 0 ? 1.0 / (double)l : lane == 1 ? 1.0 / ((double)l - 1.0) : 1.0 / ((double)l + 1.0);
+          double r = 0.0;
+          if (__any_sync(0xffffffffu, need)) r = need ? 1.0 / (pow(base, ex) + ADDON) : 0.0;
+          if (lane < 3) C.sh->red[NWARP + 2 + lane] = r;
+        }
         __syncthreads();
         int which = 0;  // 0: keep q, -1: lower, +1: raise
-        const bool sel = (d.nqwait == 0);
-        double etaqm1 = 0.0, etaqp1 = 0.0;
+        const double etaq = C.sh->red[NWARP + 2];
+        double etaqm1 = C.sh->red[NWARP + 3], etaqp1 = C.sh->red[NWARP + 4];
         if (sel) {
-          if (d.nq != 1) {
-            const double ddn = bnorm(yh + (size_t)(d.l - 1) * n, C.ewt, n, C.sh->red) / d.tq[1];
-            etaqm1 = 1.0 / (pow(BIAS1 * ddn, 1.0 / (flotl - 1.0)) + ADDON);
-          }
-          if (d.l != d.lmax) {
-            const double cnquot = (d.tq[5] / d.conp) * pow(d.h / d.tau[2], (double)d.l);
-            for (int i = tid; i < n; i += NT) C.savf[i] = C.acor[i] - cnquot * yh[(size_t)(d.lmax - 1) * n + i];
-            const double dup = bnorm(C.savf, C.ewt, n, C.sh->red) / d.tq[3];
-            etaqp1 = 1.0 / (pow(BIAS3 * dup, 1.0 / (flotl + 1.0)) + ADDON);
-          }
-          if (d.etaq >= etaqp1) which = (d.etaq < etaqm1) ? -1 : 0;
+          if (etaq >= etaqp1) which = (etaq < etaqm1) ? -1 : 0;
           else which = (etaqp1 > etaqm1) ? 1 : -1;
           if (which == 1) {
             for (int i = tid; i < n; i += NT) yh[(size_t)(d.lmax - 1) * n + i] = C.acor[i];
@@ -496,6 +558,7 @@ __device__ void dv_step(Ctx<T>& C) {
         }
         __syncthreads();
         if (tid == 0) {
+          d.etaq = etaq;
           if (sel) { d.nqwait = 2; d.etaqm1 = etaqm1; }
           if (which == 0) { d.eta = d.etaq; d.newq = d.nq; }
           else if (which == -1) { d.eta = d.etaqm1; d.newq = d.nq - 1; }
@@ -515,7 +578,7 @@ __device__ void dv_step(Ctx<T>& C) {
         d.etamax = (d.nst <= 10) ? ETAMX2 : ETAMX3;
       }
       {
-        const double r = 1.0 / d.tq[2];
+        const double r = d.rtq2;
         for (int i = tid; i < n; i += NT) C.acor[i] = r * C.acor[i];
       }
       __syncthreads();

@@ -123,8 +123,12 @@ __device__ double h2_photo_s(double nh2, const SysPhys& S) {
 // lanes.  All 32 lanes must call; the result is returned in every lane.
 __device__ double co_photo_w(double nh2, double nco, const SysPhys& S) {
   const int lane = threadIdx.x & 31;
-  const double lu = log10(fabs(nco) + 1.0), lw = log10(fabs(nh2) + 1.0);
-  double lognco = log10(nco + 1.0), lognh2 = log10(nh2 + 1.0);
+  // the four logarithms in four lanes of one warp-wide evaluation (FP64
+  // issue is per warp instruction, so this costs one log10, not four)
+  const double larg = lane == 0 ? fabs(nco) + 1.0 : lane == 1 ? fabs(nh2) + 1.0 : lane == 2 ? nco + 1.0 : nh2 + 1.0;
+  const double lg = log10(larg);
+  const double lu = __shfl_sync(0xffffffffu, lg, 0), lw = __shfl_sync(0xffffffffu, lg, 1);
+  double lognco = __shfl_sync(0xffffffffu, lg, 2), lognh2 = __shfl_sync(0xffffffffu, lg, 3);
   if (lognco < cK.nco_grid[0]) lognco = cK.nco_grid[0];
   if (lognh2 < cK.nh2_grid[0]) lognh2 = cK.nh2_grid[0];
   if (lognco > cK.nco_grid[6]) lognco = cK.nco_grid[6];
@@ -152,21 +156,20 @@ __device__ double co_photo_w(double nh2, double nco, const SysPhys& S) {
     if (jlo == j) { ya = v[j]; yb = v[j + 1]; ya2 = w2[j]; yb2 = w2[j + 1]; }
   const double a = (cK.nco_grid[jlo + 1] - lognco), b = (lognco - cK.nco_grid[jlo]);
   const double val = a * ya + b * yb + ((a * a * a - a) * ya2 + (b * b * b - b) * yb2) / 6.0;
-  const double ssf = exp(val * 2.302585092994045684);
   double lb = (5675.0 - 200.6 * lw) - (571.6 - 24.09 * lw) * lu + (18.22 - 0.7664 * lw) * (lu * lu);
   if (lb > 1076.1) lb = 1076.1;
   if (lb < 913.6) lb = 913.6;
   const double tl = S.avt * xlambda(lb);
-  // scatter: lanes 1..5 take one exponential each
+  // all exponentials in one warp-wide evaluation: lanes 1..5 the scattering
+  // terms (lane 0 when tl < 1), lane 7 the shielding factor 10^val
   const double c[6] = {1.0, 2.006, -1.438, 7.364e-01, -5.076e-01, -5.920e-02};
   const double k1[6] = {7.514e-01, 8.490e-01, 1.013, 1.282, 2.005, 5.832};
-  double term = 0.0;
-  if (tl < 1.0) {
-    if (lane == 0) { const double e = k1[0] * tl; if (e < 100.0) term = c[0] * exp(-e); }
-  } else if (lane >= 1 && lane < 6) {
-    const double e = k1[lane] * tl;
-    if (e < 100.0) term = c[lane] * exp(-e);
-  }
+  const int sl = lane < 6 ? lane : 0;
+  const double e = k1[sl] * tl;
+  const bool use = (tl < 1.0) ? (lane == 0) : (lane >= 1 && lane < 6);
+  const double x = exp(lane == 7 ? val * 2.302585092994045684 : -e);
+  const double term = (use && e < 100.0) ? c[sl] * x : 0.0;
+  const double ssf = __shfl_sync(0xffffffffu, x, 7);
   double sca = 0.0;
 #pragma unroll
   for (int j = 0; j < 6; j++) sca += __shfl_sync(0xffffffffu, term, j);

@@ -40,22 +40,24 @@ static_assert(LuCfg<float>::NB <= LU_NB_MAX && LuCfg<double>::NB <= LU_NB_MAX, "
 
 
 // P = I + con * J over an n x n row-major matrix: 16-byte vector loads issued
-// four at a time so the L2 round trips overlap.  n*n must be a multiple of
-// the vector width (n even).
+// eight at a time per thread so the memory round trips overlap (J is often
+// no longer in L2 when P is re-formed).  n*n must be a multiple of the
+// vector width (n even).
 template <typename T>
 __device__ void form_newton_matrix(const T* __restrict__ J, T* __restrict__ P, int n, T con) {
   using V = typename Vec2<T>::type;
   constexpr int W = Vec2<T>::W;
+  constexpr int U = 8;
   const int nv = (n * n) / W;
   const V* __restrict__ Jv = reinterpret_cast<const V*>(J);
   V* __restrict__ Pv = reinterpret_cast<V*>(P);
   int i = threadIdx.x;
-  for (; i + 3 * NT < nv; i += 4 * NT) {
-    V a[4];
+  for (; i + (U - 1) * NT < nv; i += U * NT) {
+    V a[U];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) a[u] = Jv[i + u * NT];
+    for (int u = 0; u < U; ++u) a[u] = Jv[i + u * NT];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < U; ++u) {
       T* e = reinterpret_cast<T*>(&a[u]);
 #pragma unroll
       for (int w = 0; w < W; ++w) e[w] *= con;
