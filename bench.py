@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--warmup-final-time", type=float, default=1e3, help="finalTime (yr) of warm-up models")
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
     ap.add_argument("--final-time", type=float, default=1e6, help="finalTime (yr) of the grid models")
+    ap.add_argument("--serve", type=int, default=0, help="serving run: number of Poisson-arriving requests")
+    ap.add_argument("--rate", type=float, default=20.0, help="serving arrival rate (requests/s)")
     ap.add_argument("--kernel", default="solve", choices=["solve", "lu"],
                     help="lu: time the batched Newton-matrix LU alone (--models matrices)")
     return ap.parse_args()
@@ -185,7 +187,7 @@ def reference_arm(args):
     v = float(np.mean(vals))
     cb["value"] = v
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.cpu_seconds, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": workload(args.models, args.final_time), "models": args.models, "seed": SEED},
             "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -389,8 +391,67 @@ def lu_kernel(args):
     ctx.close()
 
 
+def serve_requests(n: int, seed: int = SEED):
+    """The serving mix: 70% static CLOUD, 30% freefall collapse 1e2 -> 1e6
+    cm^-3, finalTime 10^U(4,7) yr, other parameters drawn as in the grid."""
+    from uclchem_gb300.params import grid_params
+    rng = np.random.default_rng(seed + 5)
+    reqs = grid_params(n, seed=seed + 7, final_time=1e6)
+    for d in reqs:
+        d["finalTime"] = float(10 ** rng.uniform(4, 7))
+        if rng.uniform() < 0.3:
+            d.update({"freefall": True, "initialDens": 1e2, "finalDens": 1e6})
+    return reqs
+
+
+def serve_arm(args):
+    """Poisson request stream through ucl_serve_models_device: requests are
+    admitted on the device at their arrival times; p50/p99 latency (arrival
+    to completion) and completed models/s."""
+    import torch
+    from uclchem_gb300 import _lib, network
+    from uclchem_gb300.params import make_param_array
+    ctx = _lib.Context(network.DEFAULT_BLOB, device=0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    n, rows = args.serve, 160
+    reqs = serve_requests(n)
+    params = make_param_array(reqs)
+    rng = np.random.default_rng(SEED + 11)
+    arrival = np.cumsum(rng.exponential(1.0 / args.rate, n))
+    dev = torch.device("cuda", 0)
+    p_d = torch.from_numpy(params.view(np.uint8).reshape(n, -1).copy()).to(dev)
+    a_d = torch.from_numpy(arrival).to(dev)
+    ph = torch.empty((n, rows, 8), dtype=torch.float64, device=dev)
+    ab = torch.empty((n, rows, ctx.nspec), dtype=torch.float64, device=dev)
+    nr = torch.empty(n, dtype=torch.int32, device=dev)
+    fl = torch.empty(n, dtype=torch.int32, device=dev)
+    sd = torch.empty((n, _lib.STATS_DTYPE.itemsize), dtype=torch.uint8, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ctx.serve_models_device(n, p_d.data_ptr(), a_d.data_ptr(), None, rows, ph.data_ptr(), ab.data_ptr(),
+                            nr.data_ptr(), fl.data_ptr(), sd.data_ptr(), _lib.PREC_MIXED, 0, stream.cuda_stream)
+    e1.record(stream)
+    stream.synchronize()
+    ms = e0.elapsed_time(e1)
+    st = sd.cpu().numpy().view(_lib.STATS_DTYPE).reshape(n)
+    flags = fl.cpu().numpy()
+    lat = st["latency_ms"]
+    print(json.dumps({"mode": "serving", "requests": n, "arrival_rate_per_s": args.rate,
+                      "mix": "70% static CLOUD, 30% freefall 1e2->1e6; finalTime 10^U(4,7) yr",
+                      "models_per_s": n / (ms / 1e3), "wall_ms": ms,
+                      "p50_latency_ms": float(np.percentile(lat, 50)), "p99_latency_ms": float(np.percentile(lat, 99)),
+                      "p50_queue_ms": float(np.percentile(st["queue_ms"], 50)),
+                      "p99_queue_ms": float(np.percentile(st["queue_ms"], 99)),
+                      "failed": int((flags != 0).sum()), "slots": ctx.slots(_lib.PREC_MIXED)}), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
+    if args.serve > 0:
+        serve_arm(args)
+        return
     if args.kernel == "lu":
         lu_kernel(args)
     elif args.impl == "reference":
