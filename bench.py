@@ -74,6 +74,23 @@ def dist_info():
 
 
 # --------------------------------------------------------------------------
+def max_over_ranks(ms: float, device, world: int) -> float:
+    """The job's time is the slowest rank's (one replica per GPU, no data
+    exchange between them)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_models_per_s(models_per_rank: int, world: int, steps: int, ms: float) -> float:
+    """Whole-job throughput: every rank integrates its own grid sample."""
+    return models_per_rank * world * steps / (ms / 1e3)
+
+
 class ClockSampler:
     """nvidia-smi clocks/throttle reasons sampled while the timed region runs."""
 
@@ -253,13 +270,9 @@ def our_arm(args):
     barrier()
     wall = time.time() - t0
     clocks = clk.stop()
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dev, world)
     ms_per_step = ms / args.steps
-    value = M * world * args.steps / (ms / 1e3)
+    value = job_models_per_s(M, world, args.steps, ms)
     stats = st_d.cpu().numpy().view(_lib.STATS_DTYPE).reshape(M)
     flags = fl_d.cpu().numpy()
     nrows = nr_d.cpu().numpy()
