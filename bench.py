@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--warmup-final-time", type=float, default=1e3, help="finalTime (yr) of warm-up models")
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
     ap.add_argument("--final-time", type=float, default=1e6, help="finalTime (yr) of the grid models")
+    ap.add_argument("--dump", default="", help="write per-model parameters, flags and device stats of the "
+                                                "timed step to this .npz")
     ap.add_argument("--serve", type=int, default=0, help="serving run: number of Poisson-arriving requests")
     ap.add_argument("--rate", type=float, default=20.0, help="serving arrival rate (requests/s)")
     ap.add_argument("--kernel", default="solve", choices=["solve", "lu"],
@@ -276,6 +278,8 @@ def our_arm(args):
     stats = st_d.cpu().numpy().view(_lib.STATS_DTYPE).reshape(M)
     flags = fl_d.cpu().numpy()
     nrows = nr_d.cpu().numpy()
+    if args.dump and rank == 0:
+        np.savez(args.dump, params=params, flags=flags, nrows=nrows, stats=stats)
     lat = stats["solve_ms"]
 
     # work counted by the device (for the roofline of the megakernel)
