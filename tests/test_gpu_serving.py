@@ -58,6 +58,12 @@ def test_serving_matches_batch_and_times_are_consistent():
         r = int(bnr[k])
         np.testing.assert_array_equal(bab[k, :r], sab[k, :r])
         np.testing.assert_array_equal(bph[k, :r], sph[k, :r])
+    # batch admission is longest-expected first: the max_ctas highest-key
+    # models (log10 n + 0.05 T) start at once
+    bst = out["batch"][4]
+    key = np.log10(params["initialDens"]) + 0.05 * params["initialTemp"]
+    first = np.argsort(-key.astype(np.float32), kind="stable")[:4]
+    assert (bst["queue_ms"][first] < 5.0).all()
     # latency = queueing + service; requests start no earlier than arrival
     assert (sst["queue_ms"] >= 0).all()
     np.testing.assert_allclose(sst["latency_ms"], sst["queue_ms"] + sst["solve_ms"], atol=0.5)

@@ -776,7 +776,8 @@ static int solve_dev(ucl_ctx* c, int nmodels, const ucl_model_params* params_d, 
                j_b = a256((size_t)nslots * n * n * sizeof(T)), perm_b = a256((size_t)nslots * n * 4),
                scr_b = a256((size_t)nslots * 2 * LuCfg<T>::NB * n * sizeof(T)),
                dinv_b = a256((size_t)nslots * dinv_elems(n) * sizeof(T));
-  int rc = c->ws.ensure(yh_b + rate_b + 2 * j_b + perm_b + scr_b + dinv_b + 512);
+  const size_t order_b = a256((size_t)nmodels * 4);
+  int rc = c->ws.ensure(yh_b + rate_b + 2 * j_b + perm_b + scr_b + dinv_b + 512 + order_b);
   if (rc) return rc;
   char* base = (char*)c->ws.p;
   SlotArrays<T> A;
@@ -789,11 +790,18 @@ static int solve_dev(ucl_ctx* c, int nmodels, const ucl_model_params* params_d, 
   A.dinv = (T*)(base + yh_b + rate_b + 2 * j_b + perm_b + scr_b);
   int* counter = (int*)(base + yh_b + rate_b + 2 * j_b + perm_b + scr_b + dinv_b);
   unsigned long long* epoch = (unsigned long long*)((char*)counter + 16);
+  int* order = (int*)((char*)counter + 512);
   if (cudaMemsetAsync(counter, 0, 32, c->stream) != cudaSuccess) return UCL_E_CUDA;
+  // a batch (no arrival schedule) is admitted longest-expected first
+  if (!arrival_d && nmodels > nslots) {
+    k_order<<<1, 1024, 0, c->stream>>>(params_d, nmodels, order);
+    if (cudaGetLastError() != cudaSuccess) return UCL_E_CUDA;
+  }
   const SmemLayout L = smem_layout<T>(n, c->nreac, c->tab.nchunk);
   k_solve_models<T><<<nslots, NT, L.total, c->stream>>>(c->tab.dn, params_d, start_d, nmodels, max_rows, phys_d,
                                                        abund_d, nrows_d, flags_d, stats_d, A, counter,
-                                                       epoch, arrival_d);
+                                                       epoch, arrival_d,
+                                                       (!arrival_d && nmodels > nslots) ? order : nullptr);
   return cuda_status(cudaGetLastError());
 }
 

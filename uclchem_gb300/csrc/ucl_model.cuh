@@ -310,8 +310,54 @@ __device__ __forceinline__ Slot<T> slot_of(const SlotArrays<T>& A, int s, int n,
 // bounded wait of the admission loop: at most this many sleeps of 20 us
 constexpr unsigned ADMIT_SLEEP_LIMIT = 1u << 26;
 
+// Admission order of a batch: longest-expected first, so that the slowest
+// models do not start last and set the makespan.  The expected cost grows
+// with density and temperature (faster grain-surface chemistry makes the
+// system stiffer); the key is log10(n) + 0.05 T.  Results of each model do
+// not depend on the order.  Batches above ORDER_MAX keep index order.
+constexpr int ORDER_MAX = 4096;
+__global__ void __launch_bounds__(1024) k_order(const ucl_model_params* params, int nmodels, int* order) {
+  __shared__ float key[ORDER_MAX];
+  __shared__ int idx[ORDER_MAX];
+  const int tid = threadIdx.x;
+  if (nmodels > ORDER_MAX) {
+    for (int i = tid; i < nmodels; i += blockDim.x) order[i] = i;
+    return;
+  }
+  int P = 1;
+  while (P < nmodels) P <<= 1;
+  for (int i = tid; i < P; i += blockDim.x) {
+    if (i < nmodels) {
+      key[i] = (float)(log10(params[i].initialDens) + 0.05 * params[i].initialTemp);
+      idx[i] = i;
+    } else {
+      key[i] = -INFINITY;
+      idx[i] = 0x7fffffff;
+    }
+  }
+  __syncthreads();
+  // bitonic sort into "before" order: larger key first, then smaller index
+  auto before = [&](int a, int b) { return key[a] > key[b] || (key[a] == key[b] && idx[a] < idx[b]); };
+  for (int k = 2; k <= P; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = tid; i < P; i += blockDim.x) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const bool up = (i & k) == 0;
+          if (up ? before(ixj, i) : before(i, ixj)) {
+            const float tk = key[i]; key[i] = key[ixj]; key[ixj] = tk;
+            const int ti = idx[i]; idx[i] = idx[ixj]; idx[ixj] = ti;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int i = tid; i < nmodels; i += blockDim.x) order[i] = idx[i];
+}
+
 // Persistent solver: each CTA pulls model indices from a device counter
-// (requests in index order).  The launch epoch is the first CTA's start
+// (requests in index order, or through `order` when given).  The launch epoch is the first CTA's start
 // time.  With an arrival schedule (seconds after the epoch, ascending), a
 // request is not started before its arrival; queue and latency times are
 // measured from arrival (from the epoch without a schedule).
@@ -320,7 +366,7 @@ __global__ void __launch_bounds__(NT, 1) k_solve_models(DevNet N, const ucl_mode
                                                      int nmodels, int max_rows, double* phys_out, double* abund_out,
                                                      int* nrows_out, int* flag_out, ucl_model_stats* stats,
                                                      SlotArrays<T> ws, int* counter, unsigned long long* epoch,
-                                                     const double* arrival_s) {
+                                                     const double* arrival_s, const int* order) {
   extern __shared__ __align__(16) char smem[];
   __shared__ Shared sh;
   __shared__ DevNet sN;
@@ -337,7 +383,8 @@ __global__ void __launch_bounds__(NT, 1) k_solve_models(DevNet N, const ucl_mode
   }
   for (;;) {
     if (threadIdx.x == 0) {
-      sh.ms.model = atomicAdd(counter, 1);
+      const int k = atomicAdd(counter, 1);
+      sh.ms.model = (order && k < nmodels) ? order[k] : k;
       const int mi = sh.ms.model;
       sh.ms.ta = t_epoch;
       if (mi < nmodels && arrival_s) {
