@@ -261,7 +261,7 @@ __device__ void dv_set_w(DvState& d) {
   const int nq = d.nq, l = d.l;
   const double flotl = (double)l;
   const double kR[8] = {0.0, 1.0, 1.0 / 2.0, 1.0 / 3.0, 1.0 / 4.0, 1.0 / 5.0, 1.0 / 6.0, 1.0 / 7.0};
-  // round 1: lane j (1..nq) forms hsum_j = h + tau[1] + ... + tau[j] and h/hsum_j
+  // first division step: lane j (1..nq) forms hsum_j = h + tau[1] + ... + tau[j] and h/hsum_j
   double hs = d.h;
   for (int j = 1; j <= nq; ++j)
     if (j <= lane) hs = hs + d.tau[j];
@@ -301,7 +301,7 @@ __device__ void dv_set_w(DvState& d) {
   const double rxn = rx[nq];  // h / hsum_nq, for the order-raise constant
   const double t5 = alph0 - kR[nq + 1];
   const double t6 = ahatn0 - rxn;
-  // round 2: independent quotients
+  // second division step: independent quotients
   double num, den;
   switch (lane) {
     case 0: num = alph0 * t2; den = t1; break;           // tq[2]
@@ -315,7 +315,7 @@ __device__ void dv_set_w(DvState& d) {
   const double q_tq2 = __shfl_sync(0xffffffffu, q2, 0), q_b = __shfl_sync(0xffffffffu, q2, 1);
   const double q_cnqm1 = __shfl_sync(0xffffffffu, q2, 2), q_elp1 = __shfl_sync(0xffffffffu, q2, 3);
   const double q_elp2 = __shfl_sync(0xffffffffu, q2, 4), rl1 = __shfl_sync(0xffffffffu, q2, 5);
-  // round 3: the quotients of quotients
+  // third division step: the quotients of quotients
   if (lane == 0) { num = t2; den = q_b; }
   else if (lane == 1) { num = q_elp1; den = q_cnqm1; }
   else { num = rl1; den = d.prl1; }
