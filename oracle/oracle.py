@@ -141,3 +141,44 @@ def initial_abundances(oracle: Oracle, param_dict=None):
     d["finalTime"] = 0.0
     phys, ab, flag, _ = oracle.cloud(d, max_rows=2)
     return ab[0], phys[0]
+
+
+class MassActionOracle:
+    """The oracle's DVODE on a generic mass-action network (a
+    uclchem_gb300.synthetic.SyntheticNetwork): flux_r = k_r y_a [n y_b]."""
+
+    def __init__(self, net):
+        lib = ctypes.CDLL(_build.build())
+        args = [ctypes.c_int, ctypes.c_int, _ip, _ip, _dp, ctypes.c_double, _ip, _ip, _ip]
+        lib.orc_ma_rhs.argtypes = args + [_dp, _dp]
+        lib.orc_ma_solve.argtypes = args + [_dp, ctypes.c_int, _dp, ctypes.c_double, ctypes.c_double,
+                                            ctypes.c_double, ctypes.c_int, _dp, _i64p]
+        self.lib = lib
+        self.net = net
+        self._ra = np.ascontiguousarray(net.reactants[:, 0], dtype=np.int32)
+        self._rb = np.ascontiguousarray(net.reactants[:, 1], dtype=np.int32)
+        self._k = np.ascontiguousarray(net.k, dtype=np.float64)
+        self._sptr = np.ascontiguousarray(net.stoich_ptr, dtype=np.int32)
+        self._srx = np.ascontiguousarray(net.stoich_rx, dtype=np.int32)
+        self._scoef = np.ascontiguousarray(net.stoich_coef, dtype=np.int32)
+
+    def _common(self):
+        return (self.net.nspec, self.net.nreac, _ptr(self._ra, _ip), _ptr(self._rb, _ip), _ptr(self._k),
+                float(self.net.density), _ptr(self._sptr, _ip), _ptr(self._srx, _ip), _ptr(self._scoef, _ip))
+
+    def rhs(self, y):
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        out = np.zeros_like(y)
+        self.lib.orc_ma_rhs(*self._common(), _ptr(y), _ptr(out))
+        return out
+
+    def solve(self, y0, tout, rtol=1e-8, atol_factor=1e-14, atol_min=1e-25, mxstep=100000):
+        """Integrate from t = 0 through the output times tout (s).  Returns
+        (abundances [len(tout), N], istate (0 = success), counters)."""
+        y = np.array(y0, dtype=np.float64)
+        tout = np.ascontiguousarray(tout, dtype=np.float64)
+        yout = np.zeros((len(tout), len(y)))
+        cnt = np.zeros(7, dtype=np.int64)
+        rc = self.lib.orc_ma_solve(*self._common(), _ptr(y), len(tout), _ptr(tout), rtol, atol_factor, atol_min,
+                                   mxstep, _ptr(yout), _ptr(cnt, _i64p))
+        return yout, int(rc), cnt

@@ -843,6 +843,10 @@ typedef struct {
   const double* atol;
   double rtol;
   chem_t* chem;
+  /* optional right-hand side other than UCLCHEM's F (generic mass-action
+   * systems); NULL = rhs_eval on chem */
+  void (*fn)(void* ctx, const double* y, double* out);
+  void* fctx;
 } dv_t;
 
 #define YH(i, j) yh[(size_t)((j)-1) * n + (i)] /* i 0-based row, j 1-based column */
@@ -856,8 +860,13 @@ static double dvnorm(int n, const double* v, const double* w) { /* dvode.f90:902
   return sqrt(s / n);
 }
 
+static void dv_rhs(dv_t* d, const double* y, double* out) {
+  if (d->fn) d->fn(d->fctx, y, out);
+  else rhs_eval(d->chem, y, out, NULL);
+}
+
 static void dv_f(dv_t* d, const double* y, double* out) {
-  rhs_eval(d->chem, y, out, NULL);
+  dv_rhs(d, y, out);
   d->nfe++;
 }
 
@@ -1024,7 +1033,7 @@ static int dvjac(dv_t* d, double* y) {
       if (r2 > r) r = r2;
       y[j] = y[j] + r;
       fac = 1.0 / r;
-      rhs_eval(d->chem, y, d->ftem, NULL);
+      dv_rhs(d, y, d->ftem);
       double* col = d->wm + (size_t)j * n;
       for (int i = 0; i < n; i++) col[i] = (d->ftem[i] - d->savf[i]) * fac;
       y[j] = yj;
@@ -1887,4 +1896,78 @@ int orc_photo_rates(const orc_net* n, const ucl_model_params* p, const double* y
   out[1] = co_photodiss_rate(h2col, cocol, c.p.radfield, c.av);
   chem_free(&c);
   return 0;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Generic mass-action systems (the synthetic networks): the same DVODE
+ * (MF=22, finite-difference Jacobian, LINPACK LU) on
+ *   ydot_i = sum_e coef_e * flux_{rx_e},  flux_r = k_r * y_a [* density * y_b]
+ * (b < 0: one-body).  Integrated interval by interval to the output times
+ * with a cold start each interval and abstol_i = max(atol_factor*y_i,
+ * atol_min), the way integrateODESystem calls DVODE (chemistry.f90:241-292),
+ * without UCLCHEM's retry loop.  Returns 0, or the failing ISTATE.         */
+typedef struct {
+  int n, m;
+  const int *ra, *rb, *sptr, *srx, *scoef;
+  const double* k;
+  double density;
+  double* flux;
+} ma_t;
+
+static void ma_rhs(void* ctx, const double* y, double* out) {
+  ma_t* a = (ma_t*)ctx;
+  for (int r = 0; r < a->m; r++) {
+    double f = a->k[r] * y[a->ra[r]];
+    if (a->rb[r] >= 0) f = f * a->density * y[a->rb[r]];
+    a->flux[r] = f;
+  }
+  for (int i = 0; i < a->n; i++) {
+    double v = 0.0;
+    for (int e = a->sptr[i]; e < a->sptr[i + 1]; e++) v = v + (double)a->scoef[e] * a->flux[a->srx[e]];
+    out[i] = v;
+  }
+}
+
+int orc_ma_rhs(int n, int m, const int* ra, const int* rb, const double* k, double density, const int* sptr,
+               const int* srx, const int* scoef, const double* y, double* ydot) {
+  ma_t a = {n, m, ra, rb, sptr, srx, scoef, k, density, (double*)calloc((size_t)m, sizeof(double))};
+  ma_rhs(&a, y, ydot);
+  free(a.flux);
+  return 0;
+}
+
+int orc_ma_solve(int n, int m, const int* ra, const int* rb, const double* k, double density, const int* sptr,
+                 const int* srx, const int* scoef, double* y, int nout, const double* tout, double rtol,
+                 double atol_factor, double atol_min, int mxstep, double* yout, int64_t* counts) {
+  ma_t a = {n, m, ra, rb, sptr, srx, scoef, k, density, (double*)calloc((size_t)m, sizeof(double))};
+  dv_t d;
+  memset(&d, 0, sizeof(d));
+  dv_alloc(&d, n);
+  d.fn = ma_rhs;
+  d.fctx = &a;
+  double* atol = (double*)calloc((size_t)n, sizeof(double));
+  dv_counts cnt;
+  memset(&cnt, 0, sizeof(cnt));
+  double t = 0.0;
+  int rc = 0;
+  for (int o = 0; o < nout && rc == 0; o++) {
+    for (int i = 0; i < n; i++) {
+      atol[i] = atol_factor * y[i];
+      if (atol[i] < atol_min) atol[i] = atol_min;
+    }
+    d.atol = atol;
+    d.rtol = rtol;
+    d.mxstep = mxstep;
+    const int istate = dvode(&d, y, &t, tout[o], &cnt);
+    if (istate < 0) rc = istate;
+    memcpy(yout + (size_t)o * n, y, sizeof(double) * (size_t)n);
+  }
+  if (counts) {
+    counts[0] = cnt.nst; counts[1] = cnt.nfe; counts[2] = cnt.nje; counts[3] = cnt.nlu;
+    counts[4] = cnt.nni; counts[5] = cnt.ncfn; counts[6] = cnt.netf;
+  }
+  free(atol);
+  free(a.flux);
+  dv_free(&d);
+  return rc;
 }
