@@ -57,7 +57,7 @@ def oracle_ma64():
     return net, MassActionOracle(net)
 
 
-def test_oracle_dvode_conserves_and_agrees_with_scipy_vode(oracle_ma64):
+def test_oracle_dvode_conserves_and_agrees_with_independent_integrators(oracle_ma64):
     scipy_integrate = pytest.importorskip("scipy.integrate")
     net, orc = oracle_ma64
     y0 = S.initial_abundances(net, 1)[0]
