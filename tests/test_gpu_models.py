@@ -105,3 +105,24 @@ def test_python_api_cloud_mirrors_reference_layout(oracle):
     phys2, chem2, _, _, flag2 = model.cloud({"initialDens": 1e4, "initialTemp": 10.0, "finalTime": 1e3},
                                              return_array=True, starting_chemistry=start)
     assert flag2 == 0 and np.allclose(chem2[0, 0, :], start, rtol=1e-6, atol=1e-20)
+
+
+def test_empty_batches_and_invalid_arguments(ctx):
+    """Edge cases at the C ABI: empty batches succeed without work; invalid
+    precision, zero output rows and unsupported LU sizes are rejected with
+    UCL_E_ARG before anything is launched."""
+    from uclchem_gb300 import _lib
+    phys, ab, nrows, flags, stats = ctx.solve_models(make_param_array([]), 8)
+    assert phys.shape == (0, 8, 8) and ab.shape[0] == 0 and len(flags) == 0
+    params = make_param_array([CONFIG1])
+    with pytest.raises(_lib.UclError, match="-101"):
+        ctx.solve_models(params, 8, precision=7)
+    with pytest.raises(_lib.UclError, match="-101"):
+        ctx.solve_models(params, 0)
+    import torch
+    m = torch.zeros((1, 338, 338), dtype=torch.float32, device="cuda")
+    perm = torch.zeros((1, 338), dtype=torch.int32, device="cuda")
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    with pytest.raises(_lib.UclError, match="-101"):
+        ctx.lu_factor_device(1, 338, _lib.PREC_MIXED, m.data_ptr(), perm.data_ptr(), info.data_ptr())
+    ctx.lu_factor_device(0, 336, _lib.PREC_MIXED, m.data_ptr(), perm.data_ptr(), info.data_ptr())
