@@ -347,7 +347,9 @@ def our_arm(args):
                  "mixed_models_per_s": S / (mix_sub_ms / 1e3), "speedup": fp64_ms / mix_sub_ms,
                  "max_dex_mixed_vs_fp64": dex, "compared": int(ok.sum())},
         "e2e": {"value": M / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-        "gpu_launches": args.steps,
+        # per step: the persistent solver, plus the admission-order sort when
+        # the batch exceeds the resident slots
+        "gpu_launches": args.steps * (2 if M > ctx.slots(_lib.PREC_MIXED) else 1),
         "clocks": clocks,
         "counters": {k: float(stats[k].mean()) for k in ("nst", "nfe", "nje", "nlu", "nni")},
         # device phase timers of the timed step (globaltimer, per call and share of model time)
