@@ -340,7 +340,8 @@ def our_arm(args):
         "vs_baseline": None, "dtype": "f64+f32",
         "data": "synthetic (seeded parameter grid; default UCLCHEM network)",
         "config": {"workload": workload(M, args.final_time), "models": M, "seed": SEED, "precision": "mixed (FP32 LU)",
-                   "l2": "working set per SM slot ~1 MB; inputs re-read from HBM each step (step >> L2 flush)"},
+                   "l2": "inputs larger than L2: 152 resident model slots x ~1.1 MB (J, P, factors, scratch) = ~167 MB "
+                      "> 129 MB L2, rewritten throughout the step; one step is one launch"},
         "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
         "failed_models": int((flags != 0).sum()),
         "fp64": {"models": S, "final_time_yr": args.subset_final_time, "fp64_models_per_s": S / (fp64_ms / 1e3),
