@@ -67,3 +67,53 @@ def test_flux_form_reproduces_term_for_term_rhs(net, oracle):
         ydot_flux = _flux_rhs(net, y, rates)
         tol = 1e-12 * np.maximum(scale, np.abs(ydot_ref)) + 1e-300
         assert np.all(np.abs(ydot_flux - ydot_ref)[:net.nspec] <= tol[:net.nspec])
+
+
+def test_committed_tables_recompile_from_makerates_outputs():
+    """The MakeRates hook is reproducible: compiling the reference's
+    network.f90 + odes.f90 gives byte-identical device tables (skipped where
+    the reference sources are not present)."""
+    import os
+    import pytest
+    from uclchem_gb300 import network
+    src = os.environ.get("UCLCHEM_FORTRAN_SRC", "/root/reference/src/fortran_src")
+    nf, of = os.path.join(src, "network.f90"), os.path.join(src, "odes.f90")
+    if not (os.path.exists(nf) and os.path.exists(of)):
+        pytest.skip("MakeRates outputs of the reference not present")
+    blob = network.compile_network(nf, of).to_blob()
+    with open(network.DEFAULT_BLOB, "rb") as f:
+        assert f.read() == blob
+
+
+def test_blob_records_are_well_formed(net):
+    """UCLNET01: magic, then name[32] | kind u32 | count u64 | data records."""
+    import struct
+    from uclchem_gb300 import network
+    data = open(network.DEFAULT_BLOB, "rb").read()
+    assert data[:8] == b"UCLNET01"
+    off, recs = 8, {}
+    while off < len(data):
+        name, kind, count = struct.unpack_from("<32sIQ", data, off)
+        off += 44
+        size = count * (4 if kind == 1 else 8)
+        assert kind in (1, 2) and off + size <= len(data)
+        recs[name.rstrip(b"\0").decode()] = (kind, count)
+        off += size
+    assert off == len(data)
+    assert recs["dims"] == (1, 3) and recs["alpha"] == (2, net.nreac)
+    assert recs["stoich_ptr"] == (1, net.nspec + 1) and recs["stoich_rx"][1] == len(net.stoich_rx)
+
+
+def test_grid_parameters_are_seeded_and_in_range():
+    from uclchem_gb300.params import grid_params
+    a, b = grid_params(4096), grid_params(4096)
+    assert a == b
+    dens = np.array([d["initialDens"] for d in a])
+    temp = np.array([d["initialTemp"] for d in a])
+    zeta = np.array([d["zeta"] for d in a])
+    rad = np.array([d["radfield"] for d in a])
+    assert 1e2 <= dens.min() and dens.max() <= 1e7 and 10 <= temp.min() and temp.max() <= 50
+    assert 1 <= zeta.min() and zeta.max() <= 1e3 and 1 <= rad.min() and rad.max() <= 1e3
+    # log-uniform: about a fifth of the points per decade of density
+    counts = np.histogram(np.log10(dens), bins=5, range=(2, 7))[0]
+    assert (np.abs(counts / 4096 - 0.2) < 0.03).all()
