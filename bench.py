@@ -88,6 +88,30 @@ def max_over_ranks(ms: float, device, world: int) -> float:
     return float(t.item())
 
 
+def full_grid_conservation(ab_d, nrows, flags, dev):
+    """Largest relative drift of the H, He, C, N, O and S totals over every
+    output row of every successful model (computed on the device), or None
+    if it cannot be formed."""
+    try:
+        import torch
+        from uclchem_gb300 import network
+        from uclchem_gb300.analysis import element_counts
+        species = network.load_default().species
+        E = np.stack([element_counts(species, e) for e in ("H", "HE", "C", "N", "O", "S")], axis=1)
+        tot = torch.matmul(ab_d, torch.from_numpy(E.astype(np.float64)).to(dev)).cpu().numpy()
+        worst = 0.0
+        for m in np.nonzero(flags == 0)[0]:
+            r = int(nrows[m])
+            if r < 2:
+                continue
+            t0 = tot[m, 0]
+            ok = t0 > 0
+            worst = max(worst, float(np.abs(tot[m, 1:r][:, ok] / t0[ok] - 1.0).max()))
+        return worst
+    except Exception:
+        return None
+
+
 def job_models_per_s(models_per_rank: int, world: int, steps: int, ms: float) -> float:
     """Whole-job throughput: every rank integrates its own grid sample."""
     return models_per_rank * world * steps / (ms / 1e3)
@@ -281,6 +305,7 @@ def our_arm(args):
     if args.dump and rank == 0:
         np.savez(args.dump, params=params, flags=flags, nrows=nrows, stats=stats)
     lat = stats["solve_ms"]
+    conservation = full_grid_conservation(ab_d, nrows, flags, dev)
 
     # work counted by the device (for the roofline of the megakernel)
     n = neq
@@ -344,6 +369,9 @@ def our_arm(args):
                       "> 129 MB L2, rewritten throughout the step; one step is one launch"},
         "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
         "failed_models": int((flags != 0).sum()),
+        # size-independent parity property over the whole timed grid: element
+        # totals (H, He, C, N, O, S) relative to each model's first row
+        "max_element_drift": conservation,
         "fp64": {"models": S, "final_time_yr": args.subset_final_time, "fp64_models_per_s": S / (fp64_ms / 1e3),
                  "mixed_models_per_s": S / (mix_sub_ms / 1e3), "speedup": fp64_ms / mix_sub_ms,
                  "max_dex_mixed_vs_fp64": dex, "compared": int(ok.sum())},
