@@ -81,3 +81,12 @@ def test_oracle_dvode_conserves_and_agrees_with_independent_integrators(oracle_m
         sel = (ys > 1e-14) | (yo[-1] > 1e-14)
         dex = np.abs(np.log10(np.maximum(ys[sel], 1e-300)) - np.log10(np.maximum(yo[-1][sel], 1e-300)))
         assert dex.max() < 1e-4, (method, dex.max())
+
+
+def test_oracle_reports_dvode_failure_codes(oracle_ma64):
+    """MXSTEP = 1 makes DVODE stop with ISTATE = -1 (too much work), which the
+    mass-action driver returns unchanged."""
+    net, orc = oracle_ma64
+    y0 = S.initial_abundances(net, 1)[0]
+    yo, rc, cnt = orc.solve(y0, [3.16e7 * 1e4], mxstep=1)
+    assert rc == -1
