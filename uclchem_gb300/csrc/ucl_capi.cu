@@ -686,7 +686,7 @@ struct ucl_ctx {
 
 template <typename T>
 static size_t slot_bytes(int n, int nreac) {
-  return (size_t)nreac * 8 + 2 * (size_t)n * n * sizeof(T) + (size_t)n * 4 +
+  return (size_t)nreac * 8 + 2 * mat_stride(n) * sizeof(T) + (size_t)n * 4 +
          (size_t)2 * LuCfg<T>::NB * n * sizeof(T) + dinv_elems(n) * sizeof(T) + 5 * 256;
 }
 
@@ -773,7 +773,7 @@ static int solve_dev(ucl_ctx* c, int nmodels, const ucl_model_params* params_d, 
   // every region 256-byte aligned (the LU uses 16-byte vector accesses)
   auto a256 = [](size_t x) { return (x + 255) / 256 * 256; };
   const size_t yh_b = 256, rate_b = a256((size_t)nslots * c->nreac * 8),
-               j_b = a256((size_t)nslots * n * n * sizeof(T)), perm_b = a256((size_t)nslots * n * 4),
+               j_b = a256((size_t)nslots * mat_stride(n) * sizeof(T)), perm_b = a256((size_t)nslots * n * 4),
                scr_b = a256((size_t)nslots * 2 * LuCfg<T>::NB * n * sizeof(T)),
                dinv_b = a256((size_t)nslots * dinv_elems(n) * sizeof(T));
   const size_t order_b = a256((size_t)nmodels * 4);

@@ -531,6 +531,11 @@ __device__ int block_lu(T* __restrict__ A, int n, int* __restrict__ perm_out, ch
   return info;
 }
 
+// elements per n x n matrix slot in batched workspaces: n*n rounded up to a
+// multiple of 4, so every slot starts 16-byte aligned (the vector loads of
+// the LU and the Newton-matrix formation) for any n
+__host__ __device__ constexpr size_t mat_stride(int n) { return ((size_t)n * n + 3) & ~(size_t)3; }
+
 // elements of the diagonal-block inverses of an n x n factorisation
 __host__ __device__ constexpr size_t dinv_elems(int n) { return (size_t)((n + 31) / 32) * 2 * 1024; }
 

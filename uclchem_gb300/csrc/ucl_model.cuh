@@ -299,8 +299,8 @@ __device__ __forceinline__ Slot<T> slot_of(const SlotArrays<T>& A, int s, int n,
   Slot<T> W;
   W.yh = nullptr;  // shared memory, set by make_ctx
   W.rate = A.rate + (size_t)s * nreac;
-  W.J = A.J + (size_t)s * n * n;
-  W.P = A.P + (size_t)s * n * n;
+  W.J = A.J + (size_t)s * mat_stride(n);
+  W.P = A.P + (size_t)s * mat_stride(n);
   W.perm = A.perm + (size_t)s * n;
   W.scr = A.scr + (size_t)s * 2 * LuCfg<T>::NB * n;
   W.dinv = A.dinv + (size_t)s * dinv_elems(n);
