@@ -1,18 +1,28 @@
 """Benchmark: models/s of the batched mixed-precision CLOUD-grid solve on one
 GB300, against the plain-FP64 GPU path, with p50/p99 per-model latency.
 
-Workload: the 4096-point static CLOUD grid (seeded log-uniform density
-1e2-1e7 cm^-3, temperature 10-50 K, zeta and radfield 1-1e3, 1e6 yr, default
-335-species network, reltol 1e-8).  One step = integrating every model of
-the grid to 1e6 yr (46 output intervals each).
+Workload: the 4096-point static CLOUD grid (seeded: density 10^U(2,7) cm^-3,
+temperature U(10,50) K, zeta and radfield 10^U(0,3); 1e6 yr; default
+335-species network; reltol 1e-8) with 501 output rows per model, the
+reference's TIMEPOINTS=500 (src/uclchem/constants.py:22).
 
-  value      models/s, mixed path, inputs and outputs resident in HBM
-  e2e        models/s through ucl_solve_models with host buffers (copies in
-             the timed region)
-  fp64       plain-FP64 path and mixed path on an identical subset (ratio
-             and max |dex| between the two)
-  cpu_baseline  the CPU oracle (C restatement of the reference solver) on
-             the host cores, on a bounded sample of the same grid
+A step is 1/K of the grid (K = --steps, default 16, so 256 models a step).
+The K steps of the timed region are admitted together into one persistent
+launch: a model's cost spans three orders of magnitude (0.1 s to ~100 s), so
+back-to-back launches per step would each wait for their slowest model,
+while one launch lets the heavy tail of one step overlap the others.
+ms_per_step = (timed region) / K.
+
+  value         models/s, mixed path, inputs and outputs resident in HBM
+  e2e           the same grid through ucl_solve_models with host buffers
+                (params copied in, every output row copied out, inside the
+                timed region)
+  fp64          the plain-FP64 path and the mixed path on the same
+                stratified sample of the grid, to 1e6 yr: makespan and
+                per-model device-time ratios, and the max |dex| between them
+  cpu_baseline  the CPU oracle (C restatement of the reference solver) on all
+                host cores, one model per process, on a seeded sample of the
+                grid stratified over density, run to completion
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -33,34 +43,36 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Models/s batched-mixed vs plain-FP64 GPU at <=0.01 dex; p50/p99 latency"
 UNIT = "models/s"
-def workload(models: int, final_time: float) -> str:
-    return (f"{models}-point static CLOUD grid (seeded), default network (335 species, 3203 reactions), "
-            f"{final_time:g} yr, reltol 1e-8")
-MAX_ROWS = 64
+SEED = 20261203
+ROWS = 501          # TIMEPOINTS + 1 (src/uclchem/constants.py:22)
 # DRAM bytes (read + write) of the mixed solver per model-step, from one ncu
 # capture (dram__bytes_read.sum + dram__bytes_write.sum) of the 152-model,
 # 1e4-yr grid launch: 113.6 GB over 152 x 4094 model-steps.  Traffic scales
 # with model-steps once the slots' working set exceeds L2.
 DRAM_BYTES_PER_MODEL_STEP = 1.83e5
-SEED = 20261203
+FALLBACK_BF16_TFLOPS = 1900.0
+
+
+def workload(models: int, final_time: float) -> str:
+    return (f"{models}-point static CLOUD grid (seeded), default network (335 species, 3203 reactions), "
+            f"{final_time:g} yr, reltol 1e-8, {ROWS} output rows per model")
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=16, help="the grid is split into this many steps")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--models", type=int, default=4096)
-    ap.add_argument("--subset", type=int, default=16, help="models in the FP64 comparison subset")
-    ap.add_argument("--subset-final-time", type=float, default=1e5,
-                    help="finalTime (yr) of the FP64-vs-mixed comparison subset")
+    ap.add_argument("--final-time", type=float, default=1e6, help="finalTime (yr) of the grid models")
+    ap.add_argument("--subset", type=int, default=64, help="models in the FP64-vs-mixed sample")
     ap.add_argument("--warmup-models", type=int, default=152, help="models per warm-up step")
     ap.add_argument("--warmup-final-time", type=float, default=1e3, help="finalTime (yr) of warm-up models")
-    ap.add_argument("--cpu-seconds", type=float, default=30.0)
-    ap.add_argument("--final-time", type=float, default=1e6, help="finalTime (yr) of the grid models")
+    ap.add_argument("--cpu-sample", type=int, default=32, help="grid models in the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer run")
     ap.add_argument("--dump", default="", help="write per-model parameters, flags and device stats of the "
-                                                "timed step to this .npz")
+                                                "timed grid (and of the FP64 sample) to this .npz")
     ap.add_argument("--serve", type=int, default=0, help="serving run: number of Poisson-arriving requests")
     ap.add_argument("--rate", type=float, default=20.0, help="serving arrival rate (requests/s)")
     ap.add_argument("--kernel", default="solve", choices=["solve", "lu"],
@@ -88,33 +100,57 @@ def max_over_ranks(ms: float, device, world: int) -> float:
     return float(t.item())
 
 
+def job_models_per_s(models_per_rank: int, world: int, ms: float) -> float:
+    """Whole-job throughput: every rank integrates its own grid."""
+    return models_per_rank * world / (ms / 1e3)
+
+
+def lu_solve_tflops(n: int, nlu: float, nni: float, ms: float) -> float:
+    """LU (2/3 n^3 per factorisation) + triangular-solve (2 n^2 per Newton
+    iteration) flops counted by the device over `ms` of kernel time."""
+    return (2.0 / 3.0 * n ** 3 * nlu + 2.0 * n * n * nni) / (ms / 1e3) / 1e12
+
+
+def element_drift(tot: np.ndarray, nrows: np.ndarray, flags: np.ndarray) -> float:
+    """Largest |total(row)/total(row 0) - 1| over the rows of successful
+    models; tot [models, rows, elements]."""
+    worst = 0.0
+    for m in np.nonzero(flags == 0)[0]:
+        r = int(nrows[m])
+        if r < 2:
+            continue
+        t0 = tot[m, 0]
+        ok = t0 > 0
+        worst = max(worst, float(np.abs(tot[m, 1:r][:, ok] / t0[ok] - 1.0).max()))
+    return worst
+
+
 def full_grid_conservation(ab_d, nrows, flags, dev):
     """Largest relative drift of the H, He, C, N, O and S totals over every
-    output row of every successful model (computed on the device), or None
-    if it cannot be formed."""
-    try:
-        import torch
-        from uclchem_gb300 import network
-        from uclchem_gb300.analysis import element_counts
-        species = network.load_default().species
-        E = np.stack([element_counts(species, e) for e in ("H", "HE", "C", "N", "O", "S")], axis=1)
-        tot = torch.matmul(ab_d, torch.from_numpy(E.astype(np.float64)).to(dev)).cpu().numpy()
-        worst = 0.0
-        for m in np.nonzero(flags == 0)[0]:
-            r = int(nrows[m])
-            if r < 2:
-                continue
-            t0 = tot[m, 0]
-            ok = t0 > 0
-            worst = max(worst, float(np.abs(tot[m, 1:r][:, ok] / t0[ok] - 1.0).max()))
-        return worst
-    except Exception:
-        return None
+    output row of every successful model (totals formed on the device)."""
+    import torch
+    from uclchem_gb300 import network
+    from uclchem_gb300.analysis import element_counts
+    species = network.load_default().species
+    E = np.stack([element_counts(species, e) for e in ("H", "HE", "C", "N", "O", "S")], axis=1)
+    Ed = torch.from_numpy(E.astype(np.float64)).to(dev)
+    tot = np.concatenate([torch.matmul(ab_d[i:i + 256], Ed).cpu().numpy() for i in range(0, ab_d.shape[0], 256)])
+    return element_drift(tot, nrows, flags)
 
 
-def job_models_per_s(models_per_rank: int, world: int, steps: int, ms: float) -> float:
-    """Whole-job throughput: every rank integrates its own grid sample."""
-    return models_per_rank * world * steps / (ms / 1e3)
+def max_dex(a_ab, a_nr, a_fl, b_ab, b_nr, b_fl, floor=1e-14):
+    """Per-model max |log10 a - log10 b| over species above `floor` in either,
+    for models that succeed in both with the same rows (NaN otherwise)."""
+    out = np.full(len(a_nr), np.nan)
+    for k in range(len(a_nr)):
+        if a_fl[k] != 0 or b_fl[k] != 0 or a_nr[k] != b_nr[k]:
+            continue
+        r = int(a_nr[k])
+        a, b = a_ab[k, :r], b_ab[k, :r]
+        sel = (a > floor) | (b > floor)
+        d = np.abs(np.log10(np.maximum(a, 1e-300)) - np.log10(np.maximum(b, 1e-300)))
+        out[k] = float(np.where(sel, d, 0.0).max()) if sel.any() else 0.0
+    return out
 
 
 class ClockSampler:
@@ -171,6 +207,10 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------------------
+# CPU baseline: the oracle, one model per spawned worker process
+_ORACLE = None
+
+
 def _cpu_one(d):
     """One model on the oracle in a worker process; returns its wall time."""
     global _ORACLE
@@ -178,61 +218,60 @@ def _cpu_one(d):
         from oracle.oracle import Oracle
         _ORACLE = Oracle()
     t = time.time()
-    _ORACLE.cloud(d, max_rows=MAX_ROWS)
+    _ORACLE.cloud(d, max_rows=ROWS)
     return time.time() - t
 
 
-_ORACLE = None
-
-
-def cpu_baseline(dicts, seconds: float, procs: int):
-    """The oracle (C restatement of the reference solver) on the host cores:
-    one model per worker process (spawned, as the reference's grid script runs
-    one model per process), grid points taken in order, counting the models
-    completed within a wall-clock window of `seconds`; unfinished models are
-    abandoned at the deadline (which favours the CPU: slow models drop out)."""
+def cpu_sample_run(dicts, idx, procs: int):
+    """Run the grid models `idx` to completion on `procs` worker processes
+    (spawned, one model per process at a time, as the reference's grid
+    script runs its models); returns (wall seconds, per-model seconds)."""
     import multiprocessing as mp
     ctx = mp.get_context("spawn")
-    pool = ctx.Pool(procs)
-    t0 = time.time()
-    done = 0
-    it = pool.imap_unordered(_cpu_one, dicts)
-    try:
-        while True:
-            left = seconds - (time.time() - t0)
-            if left <= 0:
-                break
-            it.next(timeout=left)
-            done += 1
-    except (StopIteration, mp.TimeoutError):
-        pass
-    dt = time.time() - t0
-    pool.terminate()
-    pool.join()
-    return {"value": done / dt, "unit": UNIT, "cores": procs, "kind": "port",
-            "sample": f"{done} models completed in a {dt:.1f} s window by {procs} worker processes "
-                      f"(grid points in order, one model per process)"}
+    with ctx.Pool(procs) as pool:
+        pool.map(_cpu_one, [{"initialDens": 1e4, "finalTime": 1.0}] * procs, chunksize=1)  # start-up, untimed
+        t0 = time.time()
+        # longest-expected (densest) first, so the sample's tail does not start last
+        order = sorted(idx, key=lambda i: -dicts[i]["initialDens"])
+        per = pool.map(_cpu_one, [dicts[i] for i in order], chunksize=1)
+        wall = time.time() - t0
+    return wall, per
+
+
+def cpu_baseline(dicts, size: int, procs: int):
+    from uclchem_gb300.params import stratified_sample
+    idx = stratified_sample(dicts, size, seed=SEED)
+    wall, per = cpu_sample_run(dicts, idx, procs)
+    return {"value": len(idx) / wall, "unit": UNIT, "cores": procs, "kind": "port",
+            "sample": f"{len(idx)} grid models stratified over density (one per density stratum, seeded), "
+                      f"{ROWS} rows, each run to completion; {procs} worker processes; wall {wall:.1f} s; "
+                      f"per-model CPU s: median {np.median(per):.1f}, max {max(per):.1f}",
+            "wall_s": wall}
 
 
 def reference_arm(args):
+    """The reference's CPU path (the oracle port: the reference's Fortran
+    cannot be compiled in this image) on all host cores.  The K steps are K
+    slices of a seeded density-stratified sample of the grid, all queued to
+    one process pool, like the GPU arm's one launch."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
-    from uclchem_gb300.params import grid_params
+    from uclchem_gb300.params import grid_params, stratified_sample
     dicts = grid_params(args.models, seed=SEED, final_time=args.final_time)
-    threads = os.cpu_count() or 1
-    vals = []
-    for _ in range(max(args.warmup, 0)):
-        pass  # the oracle has no warm-up state
-    for _ in range(max(args.steps, 1)):
-        cb = cpu_baseline(dicts, args.cpu_seconds, threads)
-        vals.append(cb["value"])
-    v = float(np.mean(vals))
-    cb["value"] = v
+    procs = os.cpu_count() or 1
+    idx = stratified_sample(dicts, max(args.cpu_sample, args.steps), seed=SEED)
+    wall, per = cpu_sample_run(dicts, idx, procs)
+    v = len(idx) / wall
+    cb = {"value": v, "unit": UNIT, "cores": procs, "kind": "port",
+          "sample": f"{len(idx)} grid models stratified over density (seeded), {ROWS} rows, run to completion "
+                    f"on {procs} worker processes; {args.steps} steps = slices of the sample"}
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.cpu_seconds, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": workload(args.models, args.final_time), "models": args.models, "seed": SEED},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded parameter grid; default UCLCHEM network)",
+            "config": {"workload": workload(args.models, args.final_time), "models": args.models, "seed": SEED,
+                       "sample": len(idx)},
             "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
                                         "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -247,17 +286,17 @@ def our_arm(args):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     from uclchem_gb300 import _lib, network
-    from uclchem_gb300.params import PARAMS_DTYPE, grid_params, make_param_array
+    from uclchem_gb300.params import grid_params, make_param_array, stratified_sample
 
     ctx = _lib.Context(network.DEFAULT_BLOB, device=local)
     nspec, neq = ctx.nspec, ctx.neq
-    M = args.models
+    M, K = args.models, max(1, args.steps)
     dicts = grid_params(M, seed=SEED + rank, final_time=args.final_time)
     params = make_param_array(dicts)
     dev = torch.device("cuda", local)
     p_d = torch.from_numpy(params.view(np.uint8).reshape(M, -1).copy()).to(dev)
-    phys_d = torch.empty((M, MAX_ROWS, 8), dtype=torch.float64, device=dev)
-    ab_d = torch.empty((M, MAX_ROWS, nspec), dtype=torch.float64, device=dev)
+    phys_d = torch.empty((M, ROWS, 8), dtype=torch.float64, device=dev)
+    ab_d = torch.empty((M, ROWS, nspec), dtype=torch.float64, device=dev)
     nr_d = torch.empty(M, dtype=torch.int32, device=dev)
     fl_d = torch.empty(M, dtype=torch.int32, device=dev)
     st_d = torch.empty((M, _lib.STATS_DTYPE.itemsize), dtype=torch.uint8, device=dev)
@@ -267,7 +306,7 @@ def our_arm(args):
     torch.cuda.set_stream(stream)
 
     def solve(n, prec):
-        ctx.solve_models_device(n, p_d.data_ptr(), None, MAX_ROWS, phys_d.data_ptr(), ab_d.data_ptr(),
+        ctx.solve_models_device(n, p_d.data_ptr(), None, ROWS, phys_d.data_ptr(), ab_d.data_ptr(),
                                 nr_d.data_ptr(), fl_d.data_ptr(), st_d.data_ptr(), prec, 0, stream.cuda_stream)
 
     def barrier():
@@ -278,7 +317,15 @@ def our_arm(args):
     def upload(arr):
         p_d[: arr.size].copy_(torch.from_numpy(arr.view(np.uint8).reshape(arr.size, -1).copy()))
 
-    # warm-up steps: the same kernels on the first grid points, integrated to a short time
+    def timed(n, prec):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        solve(n, prec)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1)
+
+    # warm-up steps: the same kernels on the first grid points, to a short time
     wm = min(args.warmup_models, M)
     upload(make_param_array(grid_params(M, seed=SEED + rank, final_time=args.warmup_final_time)[:wm]))
     for _ in range(args.warmup):
@@ -290,66 +337,52 @@ def our_arm(args):
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0 = time.time()
     ev0.record(stream)
-    for _ in range(args.steps):
-        solve(M, _lib.PREC_MIXED)
+    solve(M, _lib.PREC_MIXED)  # all K steps in one persistent launch
     ev1.record(stream)
     barrier()
     wall = time.time() - t0
     clocks = clk.stop()
     ms = max_over_ranks(ev0.elapsed_time(ev1), dev, world)
-    ms_per_step = ms / args.steps
-    value = job_models_per_s(M, world, args.steps, ms)
+    value = job_models_per_s(M, world, ms)
     stats = st_d.cpu().numpy().view(_lib.STATS_DTYPE).reshape(M)
     flags = fl_d.cpu().numpy()
     nrows = nr_d.cpu().numpy()
-    if args.dump and rank == 0:
-        np.savez(args.dump, params=params, flags=flags, nrows=nrows, stats=stats)
     lat = stats["solve_ms"]
     conservation = full_grid_conservation(ab_d, nrows, flags, dev)
+    mat_tflops = lu_solve_tflops(neq, float(stats["nlu"].sum()), float(stats["nni"].sum()), ms)
+    dump = {"params": params, "flags": flags, "nrows": nrows, "stats": stats}
 
-    # work counted by the device (for the roofline of the megakernel)
-    n = neq
-    lu_flop = 2.0 / 3.0 * n ** 3 * stats["nlu"].sum()
-    solve_flop = 2.0 * n * n * stats["nni"].sum()
-    mat_tflops = (lu_flop + solve_flop) / (ms_per_step / 1e3) / 1e12 / args.steps
-
-    # plain FP64 vs mixed on an identical subset (same wave structure)
+    # plain FP64 vs mixed on the same stratified sample of the grid
     S = min(args.subset, M)
-    upload(make_param_array(grid_params(M, seed=SEED + rank, final_time=args.subset_final_time)[:S]))
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    solve(S, _lib.PREC_FP64)
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    fp64_ms = e0.elapsed_time(e1)
-    f_ab = ab_d[:S].cpu().numpy()
-    f_nr = nr_d[:S].cpu().numpy()
-    f_fl = fl_d[:S].cpu().numpy()
-    e0.record(stream)
-    solve(S, _lib.PREC_MIXED)
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    mix_sub_ms = e0.elapsed_time(e1)
-    mix_ab = ab_d[:S].cpu().numpy()
-    mix_nr = nr_d[:S].cpu().numpy()
-    mix_fl = fl_d[:S].cpu().numpy()
-    ok = (f_fl == 0) & (mix_fl == 0) & (f_nr == mix_nr)
-    dex = 0.0
-    for k in np.nonzero(ok)[0]:
-        r = int(f_nr[k])
-        a, b = mix_ab[k, :r], f_ab[k, :r]
-        sel = (a > 1e-14) | (b > 1e-14)
-        if sel.any():
-            dex = max(dex, float(np.where(sel, np.abs(np.log10(np.maximum(a, 1e-300)) -
-                                                       np.log10(np.maximum(b, 1e-300))), 0).max()))
+    sub = stratified_sample(dicts, S, seed=SEED + 2)
+    upload(params[sub])
+    fp64_ms = timed(S, _lib.PREC_FP64)
+    f_st = st_d[:S].cpu().numpy().view(_lib.STATS_DTYPE).reshape(S).copy()
+    f_ab, f_nr, f_fl = ab_d[:S].cpu().numpy(), nr_d[:S].cpu().numpy(), fl_d[:S].cpu().numpy()
+    mix_ms = timed(S, _lib.PREC_MIXED)
+    m_st = st_d[:S].cpu().numpy().view(_lib.STATS_DTYPE).reshape(S).copy()
+    m_ab, m_nr, m_fl = ab_d[:S].cpu().numpy(), nr_d[:S].cpu().numpy(), fl_d[:S].cpu().numpy()
+    dex = max_dex(m_ab, m_nr, m_fl, f_ab, f_nr, f_fl)
+    both = ~np.isnan(dex)
+    dump.update(sub=np.array(sub), fp64_stats=f_st, fp64_flags=f_fl, sub_mixed_stats=m_st, sub_dex=dex)
+    del f_ab, m_ab
 
     # end to end through the host-buffer C ABI (copies inside the timed region)
-    t0 = time.time()
-    phys_h, ab_h, nr_h, fl_h, st_h = ctx.solve_models(params, MAX_ROWS, precision=_lib.PREC_MIXED)
-    e2e_s = time.time() - t0
-    h2d = params.nbytes
-    d2h = phys_h.nbytes + ab_h.nbytes + nr_h.nbytes + fl_h.nbytes + st_h.nbytes
+    e2e = None
+    if not args.no_e2e:
+        t0 = time.time()
+        phys_h, ab_h, nr_h, fl_h, st_h = ctx.solve_models(params, ROWS, precision=_lib.PREC_MIXED)
+        e2e_s = time.time() - t0
+        h2d = params.nbytes
+        d2h = phys_h.nbytes + ab_h.nbytes + nr_h.nbytes + fl_h.nbytes + st_h.nbytes
+        e2e = {"value": M * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d // K),
+               "d2h_bytes_per_step": int(d2h // K),
+               "note": "the whole grid (all K steps) in one ucl_solve_models call: params copied in, every "
+                       "output row, flag and stat copied out"}
+        del phys_h, ab_h
 
+    if args.dump and rank == 0:
+        np.savez(args.dump, **dump)
     if rank != 0:
         return
     peaks = {}
@@ -357,31 +390,42 @@ def our_arm(args):
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
-    peak = peaks.get("bf16_tflops", 1900.0)
-    cpu = cpu_baseline(dicts, args.cpu_seconds, os.cpu_count() or 1) if world == 1 else None
+    peak = float(peaks.get("bf16_tflops", FALLBACK_BF16_TFLOPS))
+    peak_src = "measured" if "bf16_tflops" in peaks else "fallback"
+    cpu = cpu_baseline(dicts, args.cpu_sample, os.cpu_count() or 1) if world == 1 else None
+    nslots = ctx.slots(_lib.PREC_MIXED)
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+        "warmup": args.warmup, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64+f32",
         "data": "synthetic (seeded parameter grid; default UCLCHEM network)",
-        "config": {"workload": workload(M, args.final_time), "models": M, "seed": SEED, "precision": "mixed (FP32 LU)",
-                   "l2": "inputs larger than L2: 152 resident model slots x ~1.1 MB (J, P, factors, scratch) = ~167 MB "
-                      "> 129 MB L2, rewritten throughout the step; one step is one launch"},
+        "config": {"workload": workload(M, args.final_time), "models": M, "seed": SEED, "rows": ROWS,
+                   "precision": "mixed (FP32 LU on tcgen05 3xTF32, FP64 elsewhere)",
+                   "step": f"1/{K} of the grid ({M // K} models); the {K} steps are admitted together into one "
+                           f"persistent launch of {nslots} model slots",
+                   "l2": "inputs larger than L2: 152 resident model slots x ~1.1 MB (J, P, factors, scratch) = "
+                         "~167 MB > 129 MB L2, rewritten throughout the launch; 5.5 GB of output rows"},
         "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+        "latency": "per-model device time from start to completion (globaltimer)",
         "failed_models": int((flags != 0).sum()),
+        "failed_codes": {str(int(c)): int((flags == c).sum()) for c in np.unique(flags[flags != 0])},
         # size-independent parity property over the whole timed grid: element
         # totals (H, He, C, N, O, S) relative to each model's first row
         "max_element_drift": conservation,
-        "fp64": {"models": S, "final_time_yr": args.subset_final_time, "fp64_models_per_s": S / (fp64_ms / 1e3),
-                 "mixed_models_per_s": S / (mix_sub_ms / 1e3), "speedup": fp64_ms / mix_sub_ms,
-                 "max_dex_mixed_vs_fp64": dex, "compared": int(ok.sum())},
-        "e2e": {"value": M / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-        # per step: the persistent solver, plus the admission-order sort when
-        # the batch exceeds the resident slots
-        "gpu_launches": args.steps * (2 if M > ctx.slots(_lib.PREC_MIXED) else 1),
+        "fp64": {"sample": f"{S} grid models stratified over density (seeded), {args.final_time:g} yr",
+                 "fp64_models_per_s": S / (fp64_ms / 1e3), "mixed_models_per_s": S / (mix_ms / 1e3),
+                 "speedup_makespan": fp64_ms / mix_ms,
+                 "speedup_model_time": float(f_st["solve_ms"].sum() / max(m_st["solve_ms"].sum(), 1e-9)),
+                 "fp64_slots": ctx.slots(_lib.PREC_FP64), "mixed_slots": nslots,
+                 "max_dex_mixed_vs_fp64": float(np.nanmax(dex)) if both.any() else None,
+                 "models_over_0.01_dex": int((dex[both] > 0.01).sum()), "compared": int(both.sum()),
+                 "failed_fp64": int((f_fl != 0).sum()), "failed_mixed": int((m_fl != 0).sum())},
+        "e2e": e2e,
+        # in the timed region: the admission-order sort and the persistent solver
+        "gpu_launches": 2 if M > nslots else 1,
         "clocks": clocks,
         "counters": {k: float(stats[k].mean()) for k in ("nst", "nfe", "nje", "nlu", "nni")},
-        # device phase timers of the timed step (globaltimer, per call and share of model time)
+        # device phase timers of the timed grid (globaltimer, per call and share of model time)
         "phase_us_per_call": {
             "rhs": 1e3 * float(stats["t_rhs_ms"].sum() / max(stats["nfe"].sum(), 1)),
             "jacobian": 1e3 * float(stats["t_jac_ms"].sum() / max(stats["nje"].sum(), 1)),
@@ -391,12 +435,17 @@ def our_arm(args):
                         for k in ("rates", "rhs", "jac", "lu", "solve")},
         "roofline": {"bound": "tensor", "achieved": mat_tflops, "peak": peak, "unit": "TFLOP/s",
                      "frac": mat_tflops / peak,
-                     "traffic": DRAM_BYTES_PER_MODEL_STEP * float(stats["nst"].sum()) / args.steps,
-                     "note": "k_solve_models: LU (2/3 n^3 per factorisation) + triangular solves (2 n^2 per "
-                             "Newton iteration) counted by the device, over the step time, against the measured "
-                             "dense bf16 peak (the LU's trailing update runs on the tensor cores); the kernel is "
-                             "latency-bound (one CTA per model, barrier-separated phases), hence the small "
-                             "fraction; traffic = DRAM bytes per model-step from one ncu capture x model-steps"},
+                     "traffic": DRAM_BYTES_PER_MODEL_STEP * float(stats["nst"].sum()),
+                     "peak_source": f"{peak_src} dense bf16 burst (MEASURED_PEAKS.json bf16_tflops"
+                                    f"{'' if peak_src == 'measured' else ' absent: recipe fallback'}); no FP32 or "
+                                    f"TF32 peak is measured on this pool, and the LU's trailing update runs as "
+                                    f"3xTF32 MMAs",
+                     "kernel": "k_solve_models<float>, one launch per timed region",
+                     "holding_bound": "latency: one 256-thread CTA per model, barrier-separated phases; ncu shows "
+                                      "issue active ~14%, no pipe above 15%, DRAM < 1% of peak",
+                     "note": "achieved = LU flops (2/3 n^3 per factorisation) + triangular-solve flops (2 n^2 per "
+                             "Newton iteration), counted by the device, over the launch's CUDA-event time; "
+                             "traffic = DRAM bytes per model-step from one ncu capture x the launch's model-steps"},
         "cpu_baseline": cpu,
         "wall_s": wall,
     }

@@ -110,7 +110,11 @@ void ucl_ctx_destroy(ucl_ctx* ctx);
  *   params   [nsys]           model parameters
  *   abund    [nsys*NEQ]       abundances + density (in/out: totals refreshed)
  *   av       [nsys]           visual extinction of each system
- *   phi      [nsys]           CR-desorption yield state (in/out, see DESIGN)
+ *   phi      [nsys]           in: the CR-desorption yield the DESCR rates use
+ *                             (the parameter, or what the previous evaluation
+ *                             left); out: the grain-assisted recombination
+ *                             parameter of the GAR rates, which the reference
+ *                             stores in the same variable (rates.f90)
  *   rates    [nsys*nreac]     out */
 int ucl_rates_batch(ucl_ctx* ctx, int nsys, const ucl_model_params* params,
                     double* abund, const double* av, double* phi,

@@ -10,7 +10,8 @@ tests use as compact .npz files next to this script:
 * freefall_cloud.npz examples/example-output/phase1-full.dat (freefall
                      collapse 1e2 -> 1e5 cm^-3, endAtFinalDensity)
 
-Usage: python tests/golden/make_golden.py [reference_root]
+Usage: python tests/golden/make_golden.py <uclchem_root>
+       (or UCLCHEM_REFERENCE_ROOT=<uclchem_root> python tests/golden/make_golden.py)
 """
 import os
 import sys
@@ -43,4 +44,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("UCLCHEM_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: make_golden.py <uclchem_root>  (or set UCLCHEM_REFERENCE_ROOT)")
+    main(root)

@@ -71,12 +71,16 @@ def test_flux_form_reproduces_term_for_term_rhs(net, oracle):
 
 def test_committed_tables_recompile_from_makerates_outputs():
     """The MakeRates hook is reproducible: compiling the reference's
-    network.f90 + odes.f90 gives byte-identical device tables (skipped where
-    the reference sources are not present)."""
+    network.f90 + odes.f90 gives byte-identical device tables.  The UCLCHEM
+    source tree is named by the UCLCHEM_REFERENCE_ROOT environment variable;
+    the test is skipped where it is unset or lacks the MakeRates outputs."""
     import os
     import pytest
     from uclchem_gb300 import network
-    src = os.environ.get("UCLCHEM_FORTRAN_SRC", "/root/reference/src/fortran_src")
+    root = os.environ.get("UCLCHEM_REFERENCE_ROOT")
+    if not root:
+        pytest.skip("UCLCHEM_REFERENCE_ROOT is not set")
+    src = os.path.join(root, "src", "fortran_src")
     nf, of = os.path.join(src, "network.f90"), os.path.join(src, "odes.f90")
     if not (os.path.exists(nf) and os.path.exists(of)):
         pytest.skip("MakeRates outputs of the reference not present")

@@ -130,6 +130,24 @@ def make_param_array(dicts: Iterable[Optional[dict]]) -> np.ndarray:
     return arr
 
 
+def stratified_sample(dicts: List[dict], size: int, seed: int = 20261203) -> List[int]:
+    """Indices of a seeded sample of `size` grid points stratified over
+    density: the points are ranked by initialDens, cut into `size` strata of
+    equal count, and one point is drawn from each stratum (density is what
+    the cost of a model grows with most)."""
+    n = len(dicts)
+    size = min(size, n)
+    if size <= 0:
+        return []
+    order = np.argsort(np.array([d["initialDens"] for d in dicts]), kind="stable")
+    rng = np.random.default_rng(seed + 1)
+    out = []
+    for k in range(size):
+        lo, hi = k * n // size, (k + 1) * n // size
+        out.append(int(order[lo + int(rng.integers(hi - lo))]))
+    return out
+
+
 def grid_params(n: int, seed: int = 20261203, final_time: float = 1.0e6,
                 extra: Optional[dict] = None) -> List[dict]:
     """The 4096-point CLOUD grid of the benchmark: seeded log-uniform density
