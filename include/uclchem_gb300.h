@@ -36,6 +36,7 @@ extern "C" {
 #define UCL_E_NET (-104)      /* network file unreadable or inconsistent     */
 #define UCL_E_UNSUPPORTED (-105) /* option outside the supported path        */
 #define UCL_E_TIMEOUT (-106)  /* a bounded device wait expired               */
+#define UCL_E_AGAIN (-107)    /* not now: take finished requests first         */
 
 /* Per-model status words: UCLCHEM's error codes, constants.f90:22-27. */
 #define UCL_PARAMETER_READ_ERROR (-1)
@@ -67,6 +68,8 @@ typedef struct ucl_model_params {
   int32_t desorb, h2desorb, crdesorb, uvdesorb, thermdesorb;
   int32_t ion, points, mxstep;
   int32_t enforceChargeConservation, improvedH2CRPDissociation;
+  int32_t cosmicRayAttenuation; /* column-density CR attenuation, physics-core.f90:121-157 */
+  int32_t ionModel;             /* 'L' or 'H' (character code), defaultparameters.f90:47 */
 } ucl_model_params;
 
 /* Fill *p with the reference defaults (defaultparameters.f90:18-119). */
@@ -101,6 +104,20 @@ typedef struct ucl_ctx ucl_ctx;
  * initializeChemistry (src/fortran_src/chemistry.f90:46-141). */
 int ucl_ctx_create(const ucl_network* net, int device, size_t hbm_budget,
                    ucl_ctx** out);
+
+/* A context holding several networks (e.g. networks of different sizes), so
+ * that one launch can integrate models of all of them
+ * (ucl_solve_models_nets_device).  Network k is nets[k].  Every per-model
+ * array of every entry point then uses the strides of the largest network:
+ * ucl_ctx_nspec() species columns, ucl_ctx_nspec()+1 start-vector entries and
+ * ucl_ctx_nreac() rate columns per row; a smaller network fills the leading
+ * part.  The single-system probes (ucl_rates_batch, ucl_rhs_batch,
+ * ucl_jac_batch) evaluate network 0.  No counterpart in the reference,
+ * whose network is fixed at compile time. */
+int ucl_ctx_create_multi(const ucl_network* const* nets, int nnets, int device,
+                         size_t hbm_budget, ucl_ctx** out);
+int ucl_ctx_nspec(const ucl_ctx* ctx); /* largest nspec of the context's networks */
+int ucl_ctx_nreac(const ucl_ctx* ctx); /* largest reaction count */
 void ucl_ctx_destroy(ucl_ctx* ctx);
 
 /* Rate coefficients for `nsys` systems.  Replaces calculateReactionRates
@@ -160,11 +177,22 @@ typedef struct ucl_model_stats {
  *   nrows_out  [nmodels] out: rows written
  *   flag_out   [nmodels] out: 0 or UCL_* per-model error code
  *   stats_out  [nmodels] out (may be NULL)
- *   precision  UCL_PREC_FP64 or UCL_PREC_MIXED */
+ *   precision  UCL_PREC_FP64 or UCL_PREC_MIXED
+ *   rates_out  [nmodels*max_rows*nreac] out, or NULL: the rates array of
+ *              returnRates (io.f90:89-93): per row the rate coefficients as
+ *              the reference's rate() holds them at output time (the
+ *              interval's calculateReactionRates values, with the H2 and CO
+ *              photodissociation rates of the last F evaluation); row 0 is
+ *              zero, as rate() is before the first interval.
+ * Per-model options the reference rejects at start-up give that model
+ * UCL_PHYSICS_INIT_ERROR and no rows: ionModel other than 'L'/'H',
+ * improvedH2CRPDissociation without cosmicRayAttenuation
+ * (physics-core.f90:55-64), and points != 1 (the reference's multi-parcel
+ * column density reads coldens(0), outside its array, physics-core.f90:80). */
 int ucl_solve_models(ucl_ctx* ctx, int nmodels, const ucl_model_params* params,
                      const double* start, int max_rows, double* phys_out,
                      double* abund_out, int* nrows_out, int* flag_out,
-                     ucl_model_stats* stats_out, int precision);
+                     ucl_model_stats* stats_out, int precision, double* rates_out);
 
 /* Same as ucl_solve_models with every array already in device memory of the
  * context's GPU (no host copies; the call only enqueues work).  `stream` is a
@@ -175,7 +203,18 @@ int ucl_solve_models_device(ucl_ctx* ctx, int nmodels, const ucl_model_params* p
                             const double* start_dev, int max_rows, double* phys_dev,
                             double* abund_dev, int* nrows_dev, int* flag_dev,
                             ucl_model_stats* stats_dev, int precision, int max_ctas,
-                            void* stream);
+                            void* stream, double* rates_dev);
+
+/* ucl_solve_models_device for a context of several networks: model i is
+ * integrated on network net_of_dev[i] (device array of indices into the
+ * context's networks), all models in one launch.  Strides as for
+ * ucl_ctx_create_multi.  A network without the UCLCHEM grain and photo
+ * terms (no ices, no self-shielded photo reactions) needs start vectors. */
+int ucl_solve_models_nets_device(ucl_ctx* ctx, int nmodels, const int* net_of_dev,
+                                 const ucl_model_params* params_dev, const double* start_dev,
+                                 int max_rows, double* phys_dev, double* abund_dev, int* nrows_dev,
+                                 int* flag_dev, ucl_model_stats* stats_dev, double* rates_dev,
+                                 int precision, int max_ctas, void* stream);
 
 /* Serving form of ucl_solve_models_device: request i (params_dev[i], ...)
  * arrives arrival_s_dev[i] seconds after the launch starts (ascending), is
@@ -188,6 +227,36 @@ int ucl_serve_models_device(ucl_ctx* ctx, int nmodels, const ucl_model_params* p
                             const double* arrival_s_dev, const double* start_dev, int max_rows,
                             double* phys_dev, double* abund_dev, int* nrows_dev, int* flag_dev,
                             ucl_model_stats* stats_dev, int precision, int max_ctas, void* stream);
+
+/* Live serving session: one persistent solve launch on its own stream,
+ * fed while it runs.  The host appends requests to a ring of `capacity`
+ * records in pinned, device-mapped memory; an idle CTA claims the next
+ * request, integrates it and flags it done.  Each record also holds the
+ * request's outputs in device memory (max_rows rows), so `capacity` is the
+ * number of requests that may be queued, running or finished-but-not-taken
+ * at once: the HBM budget of the session (capacity 0 = as many records as
+ * the context's hbm_budget holds).  A request is admitted only into a free
+ * record: ucl_server_submit returns UCL_E_AGAIN while the record it needs
+ * still holds an untaken result.  Every device wait is bounded: a CTA that
+ * finds no request for idle_timeout_s seconds (0 = 1200 s) ends, and once
+ * the solver has ended ucl_server_poll reports UCL_E_TIMEOUT.  While a session is open its context must not be
+ * destroyed.  No counterpart in the reference, which runs one model per
+ * call.  The server's calls may be made from different host threads. */
+typedef struct ucl_server ucl_server;
+int ucl_server_open(ucl_ctx* ctx, int capacity, int max_rows, int precision, int max_ctas,
+                    double idle_timeout_s, ucl_server** out);
+int ucl_server_capacity(const ucl_server* srv);
+/* queue one model; *request receives its number (0, 1, ...) */
+int ucl_server_submit(ucl_server* srv, const ucl_model_params* params, long long* request);
+/* 1: the request's outputs are complete; 0: pending; < 0: error */
+int ucl_server_poll(ucl_server* srv, long long request);
+/* copy a finished request's outputs (layout of one model of
+ * ucl_solve_models, max_rows rows) and free its record */
+int ucl_server_take(ucl_server* srv, long long request, double* phys_out, double* abund_out,
+                    int* nrows_out, int* flag_out, ucl_model_stats* stats_out);
+/* end the session: requests already submitted are still served; then the
+ * launch is waited for and everything is freed */
+int ucl_server_close(ucl_server* srv);
 
 /* Batched dense LU with partial pivoting of `nsys` row-major n x n matrices
  * in device memory (FP32 for UCL_PREC_MIXED, FP64 otherwise), in place: the
@@ -210,15 +279,17 @@ int ucl_lu_factor_device(ucl_ctx* ctx, int nsys, int n, int precision, void* mat
  * has no counterpart in the reference (DGEFA works in the caller's arrays).
  * The row-interchange scratch is a fixed static device array of
  * UCL_LU_STATIC_SCRATCH_BYTES shared by every call; at most
- * UCL_LU_STATIC_SCRATCH_BYTES / (2 * NB * n * sizeof(element)) matrices are
- * in flight at once (NB = 32 FP32, 16 FP64), the rest are taken in turn by
- * the same CTAs.  Nothing in the scratch has to start at zero.  Calls that
+ * UCL_LU_STATIC_SCRATCH_BYTES / (2 * NB * n * sizeof(element)) matrices, and
+ * no more than fit on the GPU at once, are in flight (NB = 32 FP32, 16
+ * FP64); the rest are taken in turn by the same CTAs.  Nothing in the scratch has to start at zero.  Calls that
  * overlap in time (different streams, or different host threads without
  * ordering) race on the scratch and must not be issued.  The first call on
  * each device performs the one-time set-up on that device (the scratch's
  * device address and the kernels' shared-memory limits), so make that first
- * call before any stream capture.  Uses the current device; arguments as in
- * ucl_lu_factor_device; n > 520 or n % 4 != 0 is rejected with UCL_E_ARG. */
+ * call before any stream capture; a set-up that fails is tried again by the
+ * next call.  Uses the current device; arguments as in ucl_lu_factor_device,
+ * except that a NULL `stream` is the legacy default stream (there is no
+ * context stream); n > 520 or n % 4 != 0 is rejected with UCL_E_ARG. */
 int ucl_lu_factor_device_static(int nsys, int n, int precision, void* mats_dev, int* perm_dev,
                                 int* info_dev, void* stream);
 

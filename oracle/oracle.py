@@ -37,6 +37,8 @@ class Oracle:
         lib.orc_net_set_ions.argtypes = [_vp, ctypes.c_int, _ip]
         lib.orc_cloud.restype = ctypes.c_int
         lib.orc_cloud.argtypes = [_vp, _vp, _dp, ctypes.c_int, _dp, _dp, _ip, _i64p]
+        lib.orc_cloud_rates.restype = ctypes.c_int
+        lib.orc_cloud_rates.argtypes = [_vp, _vp, _dp, ctypes.c_int, _dp, _dp, _ip, _i64p, _dp]
         lib.orc_cloud_batch.argtypes = [_vp, ctypes.c_int, _vp, _dp, ctypes.c_int, _dp, _dp, _ip, _ip, _i64p,
                                         ctypes.c_int]
         lib.orc_rates.argtypes = [_vp, _vp, _dp, ctypes.c_double, _dp, _dp]
@@ -64,17 +66,23 @@ class Oracle:
             pass
 
     # ------------------------------------------------------------------ #
-    def cloud(self, param_dict=None, start=None, max_rows: int = 501):
-        """One CLOUD model; returns (phys[rows,8], abund[rows,nspec], flag, counters)."""
-        p = make_params(param_dict)
+    def cloud(self, param_dict=None, start=None, max_rows: int = 501, rates: bool = False):
+        """One CLOUD model; returns (phys[rows,8], abund[rows,nspec], flag,
+        counters), and the rates rows [rows, nreac] when `rates` is set."""
+        p = np.array(param_dict, dtype=PARAMS_DTYPE) if isinstance(param_dict, (np.ndarray, np.void)) \
+            else make_params(param_dict)
         phys = np.zeros((max_rows, 8))
         ab = np.zeros((max_rows, self.nspec))
+        rr = np.zeros((max_rows, self.nreac)) if rates else None
         nrows = ctypes.c_int(0)
         cnt = np.zeros(9, dtype=np.int64)
         st = None if start is None else np.ascontiguousarray(start, dtype=np.float64)
-        flag = self.lib.orc_cloud(self.net, p.ctypes.data, None if st is None else _ptr(st), max_rows,
-                                  _ptr(phys), _ptr(ab), ctypes.byref(nrows), _ptr(cnt, _i64p))
+        flag = self.lib.orc_cloud_rates(self.net, p.ctypes.data, None if st is None else _ptr(st), max_rows,
+                                        _ptr(phys), _ptr(ab), ctypes.byref(nrows), _ptr(cnt, _i64p),
+                                        None if rr is None else _ptr(rr))
         n = nrows.value
+        if rates:
+            return phys[:n], ab[:n], flag, cnt, rr[:n]
         return phys[:n], ab[:n], flag, cnt
 
     def cloud_batch(self, dicts: Sequence[dict], max_rows: int = 501, nthreads: int = 0):
@@ -153,6 +161,9 @@ class MassActionOracle:
         lib.orc_ma_rhs.argtypes = args + [_dp, _dp]
         lib.orc_ma_solve.argtypes = args + [_dp, ctypes.c_int, _dp, ctypes.c_double, ctypes.c_double,
                                             ctypes.c_double, ctypes.c_int, _dp, _i64p]
+        lib.orc_ma_cloud.restype = ctypes.c_int
+        lib.orc_ma_cloud.argtypes = args + [_dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                            ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp, _dp, _ip, _i64p]
         self.lib = lib
         self.net = net
         self._ra = np.ascontiguousarray(net.reactants[:, 0], dtype=np.int32)
@@ -182,3 +193,19 @@ class MassActionOracle:
         rc = self.lib.orc_ma_solve(*self._common(), _ptr(y), len(tout), _ptr(tout), rtol, atol_factor, atol_min,
                                    mxstep, _ptr(yout), _ptr(cnt, _i64p))
         return yout, int(rc), cnt
+
+    def cloud(self, y0, final_time_yr=1e6, rtol=1e-8, atol_factor=1e-14, atol_min=1e-25, mxstep=10000,
+              max_rows=64):
+        """The network integrated as the device integrates a generic network
+        (orc_ma_cloud): density slot, CLOUD schedule to final_time_yr, retry
+        and clamp logic.  Returns (times [rows] yr, abundances [rows, N],
+        flag, counters)."""
+        y0 = np.ascontiguousarray(y0, dtype=np.float64)[: self.net.nspec]
+        yout = np.zeros((max_rows, self.net.nspec))
+        tyr = np.zeros(max_rows)
+        nrows = ctypes.c_int(0)
+        cnt = np.zeros(9, dtype=np.int64)
+        flag = self.lib.orc_ma_cloud(*self._common(), _ptr(y0), float(final_time_yr), rtol, atol_factor, atol_min,
+                                     mxstep, max_rows, _ptr(yout), _ptr(tyr), ctypes.byref(nrows), _ptr(cnt, _i64p))
+        r = nrows.value
+        return tyr[:r], yout[:r], int(flag), cnt

@@ -411,7 +411,35 @@ typedef struct {
   double h2ColToCell, coColToCell, cColToCell;
   double safeMantle, safeBulk, blr;
   double surfaceCoverage_in; /* bulkGainFromMantleBuildUp */
+  double h2CRPRate; /* physics-core.f90:15; zero before the first physics update */
 } chem_t;
+
+/* x**k, integer k >= 0, by the right-to-left binary method (Knuth TAOCP
+ * 4.6.3), as compiled Fortran evaluates a real to a variable integer power */
+static double ipow_bin(double x, int k) {
+  unsigned e = (unsigned)k;
+  double r = (e & 1u) ? x : 1.0;
+  while (e >>= 1) {
+    x = x * x;
+    if (e & 1u) r = r * x;
+  }
+  return r;
+}
+
+/* ionizationDependency's H2 dissociation part (physics-core.f90:121-157),
+ * coefficients ckLDiss / ckHDiss of physics-core.f90:29-37 */
+static double h2_crp_rate(const ucl_model_params* p, double coldens) {
+  static const double cL[10] = {1.582911005330e7, -6.465722684896e6, 1.172189025424e6, -1.237950798073e5,
+                                8.393404654312e3, -3.788811358130e2, 1.138688455029e1, -2.197136304567e-1,
+                                2.469841278950e-3, -1.232393620924e-5};
+  static const double cH[10] = {1.217227462831e7, -4.989649250304e6, 9.079152156645e5, -9.624890825395e4,
+                                6.551161486120e3, -2.968976216187e2, 8.959037875226e0, -1.735757324445e-1,
+                                1.959267277734e-3, -9.816996707980e-6};
+  const double* c = p->ionModel == 'H' ? cH : cL;
+  double s = 0.0;
+  for (int k = 0; k < 10; k++) s = s + c[k] * ipow_bin(log10(coldens), k);
+  return pow(10.0, s) * p->zeta;
+}
 
 static double sticking(double s0, double tc, double T) { /* rates.f90:370-378 */
   const double beta = 2.5;
@@ -544,6 +572,7 @@ static void calc_rates(chem_t* c, const double* abund, double safeMantle, double
   int i1, i2;
   if (range_on(n, R_CRP, &i1, &i2))
     for (int j = i1; j <= i2; j++) rate[j - 1] = n->alpha[j - 1] * p->zeta;
+  if (p->improvedH2CRPDissociation) rate[n->rx[X_H2_CRP]] = c->h2CRPRate; /* rates.f90:38-41 */
   if (range_on(n, R_PHOTON, &i1, &i2)) {
     for (int j = i1; j <= i2; j++) rate[j - 1] = n->alpha[j - 1] * exp(-n->gama[j - 1] * av) * p->radfield / SP(1.7);
     for (int j = i1; j <= i2; j++) {
@@ -1492,7 +1521,12 @@ static int chem_init(chem_t* c, const orc_net* n, const ucl_model_params* p, dou
   memset(c, 0, sizeof(*c));
   c->net = n;
   c->p = *p;
-  if (p->points != 1 || p->improvedH2CRPDissociation) return -1;
+  /* coreInitializePhysics's start-up checks (physics-core.f90:55-64); points
+   * > 1 is rejected as the device path rejects it (the reference's
+   * multi-parcel column density reads coldens(0), physics-core.f90:80) */
+  if (p->points != 1 || (p->ionModel != 'L' && p->ionModel != 'H') ||
+      (p->improvedH2CRPDissociation && !p->cosmicRayAttenuation))
+    return -1;
   c->cloudSize = (p->rout - p->rin) * PC;
   c->gasTemp = p->initialTemp;
   c->dustTemp = c->gasTemp;
@@ -1666,7 +1700,7 @@ static void update_target_time(model_t* m) { /* cloud.f90:39-51 */
     m->targetTime = SECONDS_PER_YEAR * 1.0e-7;
 }
 
-static void write_row(const chem_t* c, const model_t* m, double* phys, double* ab) {
+static void write_row(const chem_t* c, const model_t* m, double* phys, double* ab, double* rates, int row) {
   phys[0] = m->timeInYears;
   phys[1] = c->density;
   phys[2] = c->gasTemp;
@@ -1676,11 +1710,18 @@ static void write_row(const chem_t* c, const model_t* m, double* phys, double* a
   phys[6] = c->p.zeta;
   phys[7] = 1.0;
   memcpy(ab, m->abund, sizeof(double) * (size_t)c->net->nspec);
+  /* ratesarray(dtime, dstep, :) = rate(:nreac) (io.f90:89-93); rate() is
+   * zero before the first interval (chemistry.f90:136) */
+  if (rates) {
+    if (row == 0) memset(rates, 0, sizeof(double) * (size_t)c->net->nreac);
+    else memcpy(rates, c->rate, sizeof(double) * (size_t)c->net->nreac);
+  }
 }
 
-/* A whole CLOUD model (solveAbundances, wrap.f90:549-697, points=1) */
-int orc_cloud(const orc_net* n, const ucl_model_params* p, const double* start, int max_rows, double* phys,
-              double* abund_rows, int* nrows, int64_t* counters /* [9] or NULL */) {
+/* A whole CLOUD model (solveAbundances, wrap.f90:549-697, points=1), with
+ * the rows of the rates array when rates_rows is not NULL */
+int orc_cloud_rates(const orc_net* n, const ucl_model_params* p, const double* start, int max_rows, double* phys,
+                    double* abund_rows, int* nrows, int64_t* counters /* [9] or NULL */, double* rates_rows) {
   pthread_once(&g_tab_once, init_tables);
   chem_t c;
   model_t m;
@@ -1699,7 +1740,7 @@ int orc_cloud(const orc_net* n, const ucl_model_params* p, const double* start, 
   m.currentTime = 0.0;
   m.timeInYears = 0.0;
   if (max_rows < 1) flag = UCL_NOT_ENOUGH_TIMEPOINTS_ERROR;
-  else write_row(&c, &m, phys, abund_rows);
+  else write_row(&c, &m, phys, abund_rows, rates_rows, 0);
   row = 1;
   while (flag == 0 && ((p->endAtFinalDensity && c.density < p->finalDens) ||
                        (!p->endAtFinalDensity && m.timeInYears < p->finalTime))) {
@@ -1714,8 +1755,10 @@ int orc_cloud(const orc_net* n, const ucl_model_params* p, const double* start, 
     c.coldens = c.cloudSize / (double)(float)p->points * c.density;
     c.av = p->baseAv + c.coldens / 1.6e21;
     c.dustTemp = c.gasTemp;
+    if (p->cosmicRayAttenuation && p->improvedH2CRPDissociation) c.h2CRPRate = h2_crp_rate(p, c.coldens);
     if (row >= max_rows) { flag = UCL_NOT_ENOUGH_TIMEPOINTS_ERROR; break; }
-    write_row(&c, &m, phys + (size_t)row * UCL_N_PHYS, abund_rows + (size_t)row * n->nspec);
+    write_row(&c, &m, phys + (size_t)row * UCL_N_PHYS, abund_rows + (size_t)row * n->nspec,
+              rates_rows ? rates_rows + (size_t)row * n->nreac : NULL, row);
     row++;
   }
   *nrows = row;
@@ -1729,6 +1772,11 @@ int orc_cloud(const orc_net* n, const ucl_model_params* p, const double* start, 
   free(m.abund);
   free(m.abstol);
   return flag;
+}
+
+int orc_cloud(const orc_net* n, const ucl_model_params* p, const double* start, int max_rows, double* phys,
+              double* abund_rows, int* nrows, int64_t* counters /* [9] or NULL */) {
+  return orc_cloud_rates(n, p, start, max_rows, phys, abund_rows, nrows, counters, NULL);
 }
 
 /* Many models on `nthreads` host threads (models are independent). */
@@ -1970,4 +2018,106 @@ int orc_ma_solve(int n, int m, const int* ra, const int* rb, const double* k, do
   free(a.flux);
   dv_free(&d);
   return rc;
+}
+
+/* ---------------------------------------------------------------------- */
+/* A generic mass-action network integrated the way the device integrates
+ * any network: NEQ = N + 1 equations with the density in the last slot
+ * (zero derivative), fluxes k*D*y_a*y_b (two-body) and k*y_a (one-body),
+ * and the CLOUD output schedule, retry and clamp logic of a static model
+ * (cloud.f90:39-51, chemistry.f90:145-292; the same sequence as orc_cloud
+ * with a constant-rate RHS).                                              */
+typedef struct {
+  int n, m;
+  const int *ra, *rb, *sptr, *srx, *scoef;
+  const double* k;
+  double* flux;
+} mad_t;
+
+static void mad_rhs(void* ctx, const double* y, double* out) {
+  mad_t* a = (mad_t*)ctx;
+  const double D = y[a->n];
+  for (int r = 0; r < a->m; r++)
+    a->flux[r] = a->rb[r] >= 0 ? a->k[r] * D * y[a->ra[r]] * y[a->rb[r]] : a->k[r] * y[a->ra[r]];
+  for (int i = 0; i < a->n; i++) {
+    double v = 0.0;
+    for (int e = a->sptr[i]; e < a->sptr[i + 1]; e++) v = v + (double)a->scoef[e] * a->flux[a->srx[e]];
+    out[i] = v;
+  }
+  out[a->n] = 0.0;
+}
+
+int orc_ma_cloud(int n, int m, const int* ra, const int* rb, const double* k, double density, const int* sptr,
+                 const int* srx, const int* scoef, const double* y0, double final_time_yr, double rtol,
+                 double atol_factor, double atol_min, int mxstep, int max_rows, double* yout, double* tyr_out,
+                 int* nrows, int64_t* counters /* [9] or NULL */) {
+  const int neq = n + 1;
+  mad_t a = {n, m, ra, rb, sptr, srx, scoef, k, (double*)calloc((size_t)m, sizeof(double))};
+  model_t md;
+  memset(&md, 0, sizeof(md));
+  md.abund = (double*)calloc((size_t)neq, sizeof(double));
+  md.abstol = (double*)calloc((size_t)neq, sizeof(double));
+  memcpy(md.abund, y0, sizeof(double) * (size_t)n);
+  md.abund[n] = density;
+  dv_alloc(&md.dv, neq);
+  md.dv.fn = mad_rhs;
+  md.dv.fctx = &a;
+  md.abstol_factor = atol_factor;
+  int flag = 0, row = 0;
+  if (max_rows < 1) flag = UCL_NOT_ENOUGH_TIMEPOINTS_ERROR;
+  else {
+    memcpy(yout, md.abund, sizeof(double) * (size_t)n);
+    tyr_out[0] = 0.0;
+    row = 1;
+  }
+  while (flag == 0 && md.timeInYears < final_time_yr) {
+    double told = md.currentTime;
+    md.timeInYears = md.currentTime / SECONDS_PER_YEAR;
+    update_target_time(&md);
+    md.currentTime = told;
+    int loop = 0;
+    double orig = md.targetTime;
+    while (md.currentTime < md.targetTime && loop < 10) {
+      md.abund[n] = density;
+      for (int i = 0; i < neq; i++) {
+        md.abstol[i] = md.abstol_factor * md.abund[i];
+        if (md.abstol[i] < atol_min) md.abstol[i] = atol_min;
+      }
+      md.dv.atol = md.abstol;
+      md.dv.rtol = rtol;
+      md.dv.mxstep = mxstep;
+      const int istate = dvode(&md.dv, md.abund, &md.currentTime, md.targetTime, &md.cnt);
+      if (istate == -1 || istate == -4 || istate == -5)
+        md.targetTime = md.currentTime + (md.targetTime - md.currentTime) * SP(0.1);
+      else if (istate == -2)
+        md.abstol_factor = md.abstol_factor * 10.0;
+      else if (istate == -3) { flag = UCL_INT_UNRECOVERABLE_ERROR; break; }
+      for (int i = 0; i < neq; i++)
+        if (md.abund[i] < MIN_ABUND) md.abund[i] = MIN_ABUND;
+      loop++;
+      if (loop > 1) md.n_retries++;
+    }
+    if (flag < 0) break;
+    if (loop == 10) flag = UCL_INT_TOO_MANY_FAILS_ERROR;
+    if (fabs(orig - md.targetTime) < SP(0.001) * orig) md.failedIntegrationCounter = 0;
+    else md.failedIntegrationCounter++;
+    if (md.failedIntegrationCounter > 10) flag = UCL_INT_TOO_MANY_FAILS_ERROR;
+    if (flag < 0) break;
+    md.timeInYears = md.targetTime / SECONDS_PER_YEAR;
+    if (row >= max_rows) { flag = UCL_NOT_ENOUGH_TIMEPOINTS_ERROR; break; }
+    memcpy(yout + (size_t)row * n, md.abund, sizeof(double) * (size_t)n);
+    tyr_out[row] = md.timeInYears;
+    row++;
+  }
+  *nrows = row;
+  if (counters) {
+    counters[0] = md.cnt.nst; counters[1] = md.cnt.nfe; counters[2] = md.cnt.nje; counters[3] = md.cnt.nlu;
+    counters[4] = md.cnt.nni; counters[5] = md.cnt.ncfn; counters[6] = md.cnt.netf; counters[7] = row;
+    counters[8] = md.n_retries;
+  }
+  dv_free(&md.dv);
+  free(md.abund);
+  free(md.abstol);
+  free(a.flux);
+  return flag;
 }

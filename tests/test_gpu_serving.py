@@ -69,3 +69,52 @@ def test_serving_matches_batch_and_times_are_consistent():
     np.testing.assert_allclose(sst["latency_ms"], sst["queue_ms"] + sst["solve_ms"], atol=0.5)
     assert (sst["latency_ms"] >= sst["solve_ms"] - 1e-6).all()
     ctx.close()
+
+
+def test_live_server_serves_requests_submitted_while_it_runs():
+    """ucl_server_*: the persistent solver is launched first; requests are
+    appended afterwards, one at a time with pauses, through the pinned
+    request ring.  Each result equals the batch path's bit for bit; a ring
+    with every record holding an untaken result refuses a new request
+    (UCL_E_AGAIN) until one is taken; closing ends the launch cleanly."""
+    import time
+    from uclchem_gb300 import _lib, network
+    ctx = _lib.Context(network.DEFAULT_BLOB, device=0)
+    reqs = _requests()[:6]
+    params = make_param_array(reqs)
+    rows = 64
+    bph, bab, bnr, bfl, _ = ctx.solve_models(params, rows, precision=_lib.PREC_MIXED)
+    srv = _lib.Server(ctx, capacity=4, max_rows=rows, precision=_lib.PREC_MIXED, max_ctas=3, idle_timeout_s=60.0)
+    try:
+        assert srv.capacity == 4
+        time.sleep(0.5)  # the solver is idle, polling the empty ring
+        ids = []
+        for k in range(4):
+            ids.append(srv.submit(params[k]))
+            time.sleep(0.05)
+        assert ids == [0, 1, 2, 3]
+        assert srv.submit(params[4]) is None  # every record is taken by a request
+        got = {}
+        t0 = time.time()
+        while len(got) < 4 and time.time() - t0 < 300:
+            for k in ids:
+                if k not in got and srv.poll(k):
+                    got[k] = srv.take(k)
+            time.sleep(0.01)
+        assert sorted(got) == ids
+        for k in (4, 5):  # records are free again
+            assert srv.submit(params[k]) == k
+        t0 = time.time()
+        while len(got) < 6 and time.time() - t0 < 300:
+            for k in (4, 5):
+                if k not in got and srv.poll(k):
+                    got[k] = srv.take(k)
+            time.sleep(0.01)
+        for k in range(6):
+            phys, ab, nr, fl, st = got[k]
+            assert fl == 0 == bfl[k] and nr == bnr[k]
+            np.testing.assert_array_equal(ab[:nr], bab[k, :nr])
+            np.testing.assert_array_equal(phys[:nr], bph[k, :nr])
+    finally:
+        srv.close()
+    ctx.close()

@@ -90,3 +90,42 @@ def test_oracle_reports_dvode_failure_codes(oracle_ma64):
     y0 = S.initial_abundances(net, 1)[0]
     yo, rc, cnt = orc.solve(y0, [3.16e7 * 1e4], mxstep=1)
     assert rc == -1
+
+
+@pytest.mark.parametrize("n", S.SIZES)
+def test_synthetic_blob_loads_through_the_c_abi(n, tmp_path):
+    """The table compiler's form of a synthetic network (to_network) is a
+    valid UCLNET01 blob: the library's host loader reads it with the right
+    sizes, every reaction is a constant-rate two-body-range entry and the
+    flux shapes are RATE*D*Y*Y / RATE*Y."""
+    import ctypes
+    from uclchem_gb300 import _lib
+    net = S.make_network(n)
+    comp = S.to_network(net)
+    two = net.reactants[:, 1] >= 0
+    np.testing.assert_array_equal(comp.flux_shape, np.where(two, 0, 1))
+    assert comp.ranges["twobodyReacs"] == (1, net.nreac)
+    assert (comp.beta == 0).all() and (comp.gama == 0).all() and comp.extrapolate.all()
+    assert set(comp.sp.values()) == {n} and set(comp.rx.values()) == {-1}
+    path = S.write_blob(net, str(tmp_path / f"syn{n}.uclnet"))
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    assert lib.ucl_network_load(path.encode(), ctypes.byref(h)) == 0
+    try:
+        assert lib.ucl_network_nspec(h) == n and lib.ucl_network_nreac(h) == net.nreac
+    finally:
+        lib.ucl_network_free(h)
+
+
+def test_oracle_cloud_schedule_on_a_synthetic_network(oracle_ma64):
+    """orc_ma_cloud (the check for the GPU's generic-network path): the
+    CLOUD output times to 1e6 yr, success, and element/charge totals
+    conserved to 1e-10 of their largest absolute entry."""
+    net, orc = oracle_ma64
+    y0 = S.start_vectors(net, 1)[0]
+    assert y0[-1] == net.density and y0.shape == (net.nspec + 1,)
+    tyr, yout, flag, cnt = orc.cloud(y0, final_time_yr=1e6, max_rows=64)
+    assert flag == 0 and len(tyr) == 47 and tyr[-1] == 1e6 and cnt[0] > 0
+    tot = yout @ net.conserved().astype(float).T
+    scale = np.abs(yout[0][None, :] * np.abs(net.conserved()).astype(float)).sum(axis=1)
+    assert (np.abs(tot - tot[0]) / scale).max() < 1e-10

@@ -67,6 +67,7 @@ struct Slot {
   int* perm;     // [n]
   T* scr;        // [2*NB*n] row-interchange staging
   T* dinv;       // [ceil(n/32) * 2 * 1024] inverses of the diagonal blocks of L and U
+  double* jpart; // [njch] partial sums of the Jacobian's entry chunks
 };
 
 template <typename T>
@@ -128,7 +129,7 @@ __device__ int dv_jac(Ctx<T>& C) {
     __syncthreads();
     ph_begin(C.sh->ms);
     dev_jac<(sizeof(T) == 4), T>(*C.N, C.sh->P, C.sh->S, C.y, C.W.rate, C.wJ, C.wJi, C.W.J, C.flux, C.dfa,
-                                 C.dfb, C.vec, C.part, C.sh->R);
+                                 C.dfb, C.vec, C.W.jpart, C.sh->R);
     ph_end(C.sh->ms, PH_JAC);
   } else {
     if (tid == 0) d.jcur = 0;

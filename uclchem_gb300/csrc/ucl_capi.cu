@@ -102,6 +102,7 @@ extern "C" void ucl_params_default(ucl_model_params* p) {
   p->phi = 1.0e5; p->uvcreff = 1.0e-3; p->omega = SP(0.5);
   p->desorb = p->h2desorb = p->crdesorb = p->uvdesorb = p->thermdesorb = 1;
   p->ion = 2; p->points = 1; p->mxstep = 10000;
+  p->ionModel = 'L';
 }
 
 // ---------------------------------------------------------------------------
@@ -320,12 +321,15 @@ static int build_tables(const ucl_network* net, const Consts& K, DeviceTables& T
         rtype[j] = blk == R_PHOTON ? RT_PHOTON : RT_CRPHOT;
         iceflag[j] = in(bulk, re1[j]) ? 2 : in(surf, re1[j]) ? 1 : 0;
       }
+  auto rx_ok = [&](int k) { return rx[k] >= 0 && rx[k] < nr; };
   if (range_on(R_FREEZE, a, b)) {
     for (int j = a - 1; j < b; j++) rtype[j] = RT_FREEZE;
-    rtype[rx[X_EFREEZE]] = RT_EFREEZE;
-    partner[rx[X_EFREEZE]] = rx[X_HFREEZE];
-    stick[rx[X_H2FREEZE]] = 1;
-    stick[rx[X_HFREEZE]] = 2;
+    if (rx_ok(X_EFREEZE) && rx_ok(X_HFREEZE)) {
+      rtype[rx[X_EFREEZE]] = RT_EFREEZE;
+      partner[rx[X_EFREEZE]] = rx[X_HFREEZE];
+    }
+    if (rx_ok(X_H2FREEZE)) stick[rx[X_H2FREEZE]] = 1;
+    if (rx_ok(X_HFREEZE)) stick[rx[X_HFREEZE]] = 2;
   }
   if (range_on(R_DESOH2, a, b))
     for (int j = a - 1; j < b; j++) rtype[j] = RT_DESOH2;
@@ -390,9 +394,9 @@ static int build_tables(const ucl_network* net, const Consts& K, DeviceTables& T
       iceflag[j] = in(bulk, re1[j]) ? 1 : 0;
     }
   }
-  rtype[rx[X_H2FORM_CT]] = RT_H2FORM;
-  rtype[rx[X_H2FORM_ER]] = RT_ZERO;
-  rtype[rx[X_H2FORM_ERDES]] = RT_ZERO;
+  if (rx_ok(X_H2FORM_CT)) rtype[rx[X_H2FORM_CT]] = RT_H2FORM;
+  if (rx_ok(X_H2FORM_ER)) rtype[rx[X_H2FORM_ER]] = RT_ZERO;
+  if (rx_ok(X_H2FORM_ERDES)) rtype[rx[X_H2FORM_ERDES]] = RT_ZERO;
   if (net->three_phase) {
     a = rg[2 * R_BULKSWAP];
     b = rg[2 * R_BULKSWAP + 1];
@@ -433,7 +437,21 @@ static int build_tables(const ucl_network* net, const Consts& K, DeviceTables& T
   D.nsix = sp[S_NSIX]; D.nsx = sp[S_NSX]; D.nclx = sp[S_NCLX]; D.no = sp[S_NO]; D.nn = sp[S_NN];
   D.nmg = sp[S_NMG]; D.np = sp[S_NP]; D.nf = sp[S_NF]; D.nna = sp[S_NNA]; D.nli = sp[S_NLI];
   D.npah = sp[S_NPAH]; D.nd = sp[S_ND]; D.n18o = sp[S_N18O]; D.n15n = sp[S_N15N]; D.n13c = sp[S_N13C];
-  D.rx_h2hv = rx[X_H2_HV]; D.rx_cohv = rx[X_CO_HV]; D.rx_chv = rx[X_C_HV];
+  D.rx_h2hv = rx_ok(X_H2_HV) ? rx[X_H2_HV] : -1;
+  D.rx_cohv = rx_ok(X_CO_HV) ? rx[X_CO_HV] : -1;
+  D.rx_chv = rx_ok(X_C_HV) ? rx[X_C_HV] : -1;
+  D.rx_h2crp = rx_ok(X_H2_CRP) ? rx[X_H2_CRP] : -1;
+  // ion list (chemistry.f90:114-121: species whose name contains '+'), and
+  // the refractory list (chemistry.f90:196); older blobs carry neither
+  std::vector<int> ions, refr;
+  if (net->ints.count("ion_list")) ions = net->I("ion_list");
+  if (net->ints.count("refractory_list")) refr = net->I("refractory_list");
+  for (int i : ions)
+    if (i < 0 || i >= ns) return UCL_E_NET;
+  for (int i : refr)
+    if (i < 0 || i >= ns) return UCL_E_NET;
+  D.n_ion = (int)ions.size();
+  D.n_refr = (int)refr.size();
   D.n_fp = (int)fp.size();
   D.desoh2_1 = first_of(R_DESOH2); D.descr_1 = first_of(R_DESCR); D.deuvcr_1 = first_of(R_DEUVCR);
   D.therm_1 = first_of(R_THERM);
@@ -445,6 +463,7 @@ static int build_tables(const ucl_network* net, const Consts& K, DeviceTables& T
   }
   a = rg[2 * R_BULKSWAP];
   b = rg[2 * R_BULKSWAP + 1];
+  if (a > nr || b > nr || a > b) { a = 1; b = 0; }  // no bulk-swap reactions
   D.swap_lo = a - 1;
   D.swap_hi = b;
   {  // totalSwap must be the sum of the bulk-swap fluxes
@@ -549,7 +568,7 @@ static int build_tables(const ucl_network* net, const Consts& K, DeviceTables& T
   }
   D.njch = (int)jchunk.size();
   D.npart = std::max(D.nchunk, D.njch);
-  T.nchunk = D.npart;
+  T.nchunk = D.nchunk;
   // surface-swap rank-1 rows
   std::vector<int> ar_row, ar_beg, ar_end, ar_rx;
   std::vector<float> ar_coef;
@@ -582,7 +601,8 @@ static int build_tables(const ucl_network* net, const Consts& K, DeviceTables& T
   }
   D.n_ph = (int)ph_row.size();
   if (D.n_ph > NT || D.n_arow > 1000 - 0) return UCL_E_UNSUPPORTED;
-  if (fsh[D.rx_h2hv] != SH_Y || fsh[D.rx_cohv] != SH_Y) return UCL_E_UNSUPPORTED;
+  if ((D.rx_h2hv >= 0 && fsh[D.rx_h2hv] != SH_Y) || (D.rx_cohv >= 0 && fsh[D.rx_cohv] != SH_Y))
+    return UCL_E_UNSUPPORTED;
   if (sp[S_NSURFACE] != ns - 1 - 0 && false) return UCL_E_NET;
 
   // upload
@@ -639,6 +659,8 @@ static int build_tables(const ucl_network* net, const Consts& K, DeviceTables& T
   img.add(D.ar_end, ar_end);
   img.add(D.ar_rx, ar_rx);
   img.add(D.ar_coef, ar_coef);
+  img.add(D.ion_list, ions);
+  img.add(D.refr_list, refr);
   img.add(D.ph_row, ph_row);
   img.add(D.ph_c1, ph_c1);
   img.add(D.ph_c2, ph_c2);
@@ -678,26 +700,38 @@ struct ucl_ctx {
   int nsm = 0;
   size_t budget = 0;
   cudaStream_t stream = nullptr;
-  DeviceTables tab;
+  std::vector<DeviceTables> tabs;  // one per network of the context
+  DevNet* nets_d = nullptr;        // device copy of every tabs[k].dn
+  // largest NEQ-1 / NEQ / reactions over the networks: the per-model strides
+  // of every batched array and the size of the per-slot workspace
   int nspec = 0, nreac = 0, neq = 0;
+  int njch = 0;                    // largest Jacobian chunk count (per-slot partial sums)
+  size_t smem32 = 0, smem64 = 0;   // solver shared memory for the largest need
   DevBuf ws, io, small;
   int slots_fp32 = 0, slots_fp64 = 0;
 };
 
 template <typename T>
-static size_t slot_bytes(int n, int nreac) {
+static size_t slot_bytes(int n, int nreac, int njch) {
   return (size_t)nreac * 8 + 2 * mat_stride(n) * sizeof(T) + (size_t)n * 4 +
-         (size_t)2 * LuCfg<T>::NB * n * sizeof(T) + dinv_elems(n) * sizeof(T) + 5 * 256;
+         (size_t)2 * LuCfg<T>::NB * n * sizeof(T) + dinv_elems(n) * sizeof(T) + (size_t)njch * 8 + 6 * 256;
+}
+
+template <typename T>
+static size_t solver_smem(const ucl_ctx* c) {
+  size_t m = 0;
+  for (const auto& t : c->tabs) m = std::max(m, smem_layout<T>(t.dn.neq, t.dn.nreac, t.dn.nchunk).total);
+  return m;
 }
 
 template <typename T>
 static int max_slots(ucl_ctx* c) {
-  const SmemLayout L = smem_layout<T>(c->neq, c->nreac, c->tab.nchunk);
-  if (cudaFuncSetAttribute(k_solve_models<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total) !=
+  const size_t sm = sizeof(T) == 4 ? c->smem32 : c->smem64;
+  if (cudaFuncSetAttribute(k_solve_models<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
       cudaSuccess)
     return 0;
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_models<T>, NT, L.total) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_models<T>, NT, sm) != cudaSuccess)
     return 0;
   // make sure the per-thread stack covers the kernel's static local memory
   cudaFuncAttributes fa;
@@ -707,11 +741,23 @@ static int max_slots(ucl_ctx* c) {
     const size_t need = (fa.localSizeBytes + 1023) / 1024 * 1024 + 1024;
     if (cur < need) cudaDeviceSetLimit(cudaLimitStackSize, need);
   }
-  return std::max(1, per_sm) * c->nsm;
+  return per_sm * c->nsm;
 }
 
-extern "C" int ucl_ctx_create(const ucl_network* net, int device, size_t hbm_budget, ucl_ctx** out) {
-  if (!net || !out) return UCL_E_ARG;
+static void ctx_free(ucl_ctx* c) {
+  for (auto& t : c->tabs) cudaFree(t.dbuf);
+  if (c->nets_d) cudaFree(c->nets_d);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  c->ws.release();
+  c->io.release();
+  c->small.release();
+  delete c;
+}
+
+static int ctx_create(const ucl_network* const* nets, int nnets, int device, size_t hbm_budget, ucl_ctx** out) {
+  if (!nets || nnets < 1 || !out) return UCL_E_ARG;
+  for (int k = 0; k < nnets; ++k)
+    if (!nets[k]) return UCL_E_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return UCL_E_CUDA;
   if (cudaSetDevice(device) != cudaSuccess) return UCL_E_CUDA;
@@ -719,54 +765,78 @@ extern "C" int ucl_ctx_create(const ucl_network* net, int device, size_t hbm_bud
   c->device = device;
   cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
   c->budget = hbm_budget ? hbm_budget : ((size_t)8 << 30);
-  c->nspec = net->nspec;
-  c->nreac = net->nreac;
-  c->neq = net->nspec + 1;
   const Consts K = make_consts();
-  if (cudaMemcpyToSymbol(cK, &K, sizeof(K)) != cudaSuccess) { delete c; return UCL_E_CUDA; }
-  const int rc = build_tables(net, K, c->tab);
-  if (rc != UCL_OK) { delete c; return rc; }
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
-    cudaFree(c->tab.dbuf);
-    delete c;
+  if (cudaMemcpyToSymbol(cK, &K, sizeof(K)) != cudaSuccess) { ctx_free(c); return UCL_E_CUDA; }
+  for (int k = 0; k < nnets; ++k) {
+    c->tabs.emplace_back();
+    const int rc = build_tables(nets[k], K, c->tabs.back());
+    if (rc != UCL_OK) {
+      c->tabs.pop_back();
+      ctx_free(c);
+      return rc;
+    }
+    c->nspec = std::max(c->nspec, nets[k]->nspec);
+    c->nreac = std::max(c->nreac, nets[k]->nreac);
+    c->njch = std::max(c->njch, c->tabs.back().dn.njch);
+  }
+  c->neq = c->nspec + 1;
+  std::vector<DevNet> dn;
+  for (const auto& t : c->tabs) dn.push_back(t.dn);
+  if (cudaMalloc(&c->nets_d, dn.size() * sizeof(DevNet)) != cudaSuccess) { ctx_free(c); return UCL_E_NOMEM; }
+  if (cudaMemcpy(c->nets_d, dn.data(), dn.size() * sizeof(DevNet), cudaMemcpyHostToDevice) != cudaSuccess) {
+    ctx_free(c);
     return UCL_E_CUDA;
   }
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { ctx_free(c); return UCL_E_CUDA; }
+  c->smem32 = solver_smem<float>(c);
+  c->smem64 = solver_smem<double>(c);
   c->slots_fp32 = max_slots<float>(c);
   c->slots_fp64 = max_slots<double>(c);
-  if (!c->slots_fp32 || !c->slots_fp64) {
-    cudaStreamDestroy(c->stream);
-    cudaFree(c->tab.dbuf);
-    delete c;
-    return UCL_E_CUDA;
-  }
+  if (!c->slots_fp32 || !c->slots_fp64) { ctx_free(c); return UCL_E_UNSUPPORTED; }
   *out = c;
   return UCL_OK;
+}
+
+extern "C" int ucl_ctx_create(const ucl_network* net, int device, size_t hbm_budget, ucl_ctx** out) {
+  return ctx_create(&net, 1, device, hbm_budget, out);
+}
+
+extern "C" int ucl_ctx_create_multi(const ucl_network* const* nets, int nnets, int device, size_t hbm_budget,
+                                    ucl_ctx** out) {
+  return ctx_create(nets, nnets, device, hbm_budget, out);
 }
 
 extern "C" void ucl_ctx_destroy(ucl_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
-  c->ws.release();
-  c->io.release();
-  c->small.release();
-  cudaFree(c->tab.dbuf);
-  cudaStreamDestroy(c->stream);
-  delete c;
+  ctx_free(c);
 }
 
 static int cuda_status(cudaError_t e) { return e == cudaSuccess ? UCL_OK : UCL_E_CUDA; }
 
+// a SolveIO with the context's strides; the caller fills the arrays
+static SolveIO make_io(const ucl_ctx* c, int nmodels, int max_rows) {
+  SolveIO io;
+  memset(&io, 0, sizeof(io));
+  io.nmodels = nmodels;
+  io.max_rows = max_rows;
+  io.start_stride = c->neq;
+  io.ab_stride = c->nspec;
+  io.rate_stride = c->nreac;
+  io.nets = c->nets_d;
+  return io;
+}
+
 // ---------------------------------------------------------------------------
 // device-pointer solve (inputs already resident on the device)
 template <typename T>
-static int solve_dev(ucl_ctx* c, int nmodels, const ucl_model_params* params_d, const double* start_d,
-                     int max_rows, double* phys_d, double* abund_d, int* nrows_d, int* flags_d,
-                     ucl_model_stats* stats_d, int nslots_req, const double* arrival_d = nullptr) {
-  const int n = c->neq;
+static int solve_dev(ucl_ctx* c, DevBuf& wsbuf, const SolveIO& io, int nslots_req, cudaStream_t st,
+                     const double* arrival_d = nullptr, LiveQueue q = LiveQueue{}) {
+  const int n = c->neq, nmodels = io.nmodels;
   int nslots = sizeof(T) == 4 ? c->slots_fp32 : c->slots_fp64;
   if (nslots_req > 0) nslots = std::min(nslots, nslots_req);
-  const size_t per = slot_bytes<T>(n, c->nreac);
+  const size_t per = slot_bytes<T>(n, c->nreac, c->njch);
   nslots = (int)std::min<size_t>(nslots, std::max<size_t>(1, c->budget / per));
   nslots = std::min(nslots, nmodels);
   if (nslots < 1) return UCL_OK;
@@ -775,11 +845,12 @@ static int solve_dev(ucl_ctx* c, int nmodels, const ucl_model_params* params_d, 
   const size_t yh_b = 256, rate_b = a256((size_t)nslots * c->nreac * 8),
                j_b = a256((size_t)nslots * mat_stride(n) * sizeof(T)), perm_b = a256((size_t)nslots * n * 4),
                scr_b = a256((size_t)nslots * 2 * LuCfg<T>::NB * n * sizeof(T)),
-               dinv_b = a256((size_t)nslots * dinv_elems(n) * sizeof(T));
+               dinv_b = a256((size_t)nslots * dinv_elems(n) * sizeof(T)),
+               jp_b = a256((size_t)nslots * c->njch * 8);
   const size_t order_b = a256((size_t)nmodels * 4);
-  int rc = c->ws.ensure(yh_b + rate_b + 2 * j_b + perm_b + scr_b + dinv_b + 512 + order_b);
+  int rc = wsbuf.ensure(yh_b + rate_b + 2 * j_b + perm_b + scr_b + dinv_b + jp_b + 512 + order_b);
   if (rc) return rc;
-  char* base = (char*)c->ws.p;
+  char* base = (char*)wsbuf.p;
   SlotArrays<T> A;
   A.yh = (double*)base;
   A.rate = (double*)(base + yh_b);
@@ -788,97 +859,126 @@ static int solve_dev(ucl_ctx* c, int nmodels, const ucl_model_params* params_d, 
   A.perm = (int*)(base + yh_b + rate_b + 2 * j_b);
   A.scr = (T*)(base + yh_b + rate_b + 2 * j_b + perm_b);
   A.dinv = (T*)(base + yh_b + rate_b + 2 * j_b + perm_b + scr_b);
-  int* counter = (int*)(base + yh_b + rate_b + 2 * j_b + perm_b + scr_b + dinv_b);
+  A.jpart = (double*)(base + yh_b + rate_b + 2 * j_b + perm_b + scr_b + dinv_b);
+  A.n = n;
+  A.nreac = c->nreac;
+  A.njch = c->njch;
+  int* counter = (int*)(base + yh_b + rate_b + 2 * j_b + perm_b + scr_b + dinv_b + jp_b);
   unsigned long long* epoch = (unsigned long long*)((char*)counter + 16);
   int* order = (int*)((char*)counter + 512);
-  if (cudaMemsetAsync(counter, 0, 32, c->stream) != cudaSuccess) return UCL_E_CUDA;
-  // a batch (no arrival schedule) is admitted longest-expected first
-  if (!arrival_d && nmodels > nslots) {
-    k_order<<<1, 1024, 0, c->stream>>>(params_d, nmodels, order);
+  if (cudaMemsetAsync(counter, 0, 32, st) != cudaSuccess) return UCL_E_CUDA;
+  // a batch (no arrival schedule, no live queue) is admitted longest-expected first
+  const bool sorted = !arrival_d && q.cap == 0 && nmodels > nslots;
+  if (sorted) {
+    k_order<<<1, 1024, 0, st>>>(io.params, nmodels, order);
     if (cudaGetLastError() != cudaSuccess) return UCL_E_CUDA;
   }
-  const SmemLayout L = smem_layout<T>(n, c->nreac, c->tab.nchunk);
-  k_solve_models<T><<<nslots, NT, L.total, c->stream>>>(c->tab.dn, params_d, start_d, nmodels, max_rows, phys_d,
-                                                       abund_d, nrows_d, flags_d, stats_d, A, counter,
-                                                       epoch, arrival_d,
-                                                       (!arrival_d && nmodels > nslots) ? order : nullptr);
+  const size_t sm = sizeof(T) == 4 ? c->smem32 : c->smem64;
+  k_solve_models<T><<<nslots, NT, sm, st>>>(io, A, counter, epoch, arrival_d, sorted ? order : nullptr, q);
   return cuda_status(cudaGetLastError());
+}
+
+static int check_solve_args(const ucl_ctx* c, int nmodels, int max_rows, const void* params, const void* phys,
+                            const void* abund, const void* nrows, const void* flags, int precision) {
+  if (!c || nmodels < 0 || max_rows < 1 || !params || !phys || !abund || !nrows || !flags) return UCL_E_ARG;
+  if (precision != UCL_PREC_FP64 && precision != UCL_PREC_MIXED) return UCL_E_ARG;
+  return UCL_OK;
+}
+
+static int solve_device(ucl_ctx* c, const SolveIO& io, int precision, int max_ctas, void* stream,
+                        const double* arrival_d = nullptr) {
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  return precision == UCL_PREC_MIXED ? solve_dev<float>(c, c->ws, io, max_ctas, st, arrival_d)
+                                     : solve_dev<double>(c, c->ws, io, max_ctas, st, arrival_d);
 }
 
 extern "C" int ucl_solve_models_device(ucl_ctx* c, int nmodels, const ucl_model_params* params_d,
                                        const double* start_d, int max_rows, double* phys_d, double* abund_d,
                                        int* nrows_d, int* flags_d, ucl_model_stats* stats_d, int precision,
-                                       int max_ctas, void* stream) {
-  if (!c || nmodels < 0 || max_rows < 1 || !params_d || !phys_d || !abund_d || !nrows_d || !flags_d)
-    return UCL_E_ARG;
-  if (precision != UCL_PREC_FP64 && precision != UCL_PREC_MIXED) return UCL_E_ARG;
+                                       int max_ctas, void* stream, double* rates_d) {
+  int rc = check_solve_args(c, nmodels, max_rows, params_d, phys_d, abund_d, nrows_d, flags_d, precision);
+  if (rc) return rc;
   if (nmodels == 0) return UCL_OK;
-  cudaSetDevice(c->device);
-  cudaStream_t user = (cudaStream_t)stream;
-  cudaStream_t keep = c->stream;
-  if (user) c->stream = user;
-  const int rc = precision == UCL_PREC_MIXED
-                     ? solve_dev<float>(c, nmodels, params_d, start_d, max_rows, phys_d, abund_d, nrows_d, flags_d,
-                                        stats_d, max_ctas)
-                     : solve_dev<double>(c, nmodels, params_d, start_d, max_rows, phys_d, abund_d, nrows_d, flags_d,
-                                         stats_d, max_ctas);
-  c->stream = keep;
-  return rc;
+  SolveIO io = make_io(c, nmodels, max_rows);
+  io.params = params_d; io.start = start_d; io.phys = phys_d; io.abund = abund_d; io.rates = rates_d;
+  io.nrows = nrows_d; io.flags = flags_d; io.stats = stats_d;
+  return solve_device(c, io, precision, max_ctas, stream);
+}
+
+extern "C" int ucl_solve_models_nets_device(ucl_ctx* c, int nmodels, const int* net_of_dev,
+                                            const ucl_model_params* params_d, const double* start_d, int max_rows,
+                                            double* phys_d, double* abund_d, int* nrows_d, int* flags_d,
+                                            ucl_model_stats* stats_d, double* rates_d, int precision, int max_ctas,
+                                            void* stream) {
+  int rc = check_solve_args(c, nmodels, max_rows, params_d, phys_d, abund_d, nrows_d, flags_d, precision);
+  if (rc) return rc;
+  if (!net_of_dev) return UCL_E_ARG;
+  if (nmodels == 0) return UCL_OK;
+  SolveIO io = make_io(c, nmodels, max_rows);
+  io.params = params_d; io.start = start_d; io.phys = phys_d; io.abund = abund_d; io.rates = rates_d;
+  io.nrows = nrows_d; io.flags = flags_d; io.stats = stats_d; io.net_of = net_of_dev;
+  return solve_device(c, io, precision, max_ctas, stream);
 }
 
 extern "C" int ucl_solve_models(ucl_ctx* c, int nmodels, const ucl_model_params* params, const double* start,
                                 int max_rows, double* phys_out, double* abund_out, int* nrows_out, int* flag_out,
-                                ucl_model_stats* stats_out, int precision) {
-  if (!c || nmodels < 0 || max_rows < 1 || !params || !phys_out || !abund_out || !nrows_out || !flag_out)
-    return UCL_E_ARG;
-  if (precision != UCL_PREC_FP64 && precision != UCL_PREC_MIXED) return UCL_E_ARG;
+                                ucl_model_stats* stats_out, int precision, double* rates_out) {
+  int rc = check_solve_args(c, nmodels, max_rows, params, phys_out, abund_out, nrows_out, flag_out, precision);
+  if (rc) return rc;
   if (nmodels == 0) return UCL_OK;
   cudaSetDevice(c->device);
   const int n = c->neq, ns = c->nspec;
   const size_t pb = sizeof(ucl_model_params) * nmodels, sb = start ? (size_t)nmodels * n * 8 : 0,
                phb = (size_t)nmodels * max_rows * UCL_N_PHYS * 8, ab = (size_t)nmodels * max_rows * ns * 8,
-               ib = (size_t)nmodels * 4, stb = stats_out ? sizeof(ucl_model_stats) * nmodels : 0;
+               ib = (size_t)nmodels * 4, stb = stats_out ? sizeof(ucl_model_stats) * nmodels : 0,
+               rb = rates_out ? (size_t)nmodels * max_rows * c->nreac * 8 : 0;
   auto al = [](size_t x) { return (x + 255) / 256 * 256; };
-  int rc = c->io.ensure(al(pb) + al(sb) + al(phb) + al(ab) + 2 * al(ib) + al(stb) + 256);
+  rc = c->io.ensure(al(pb) + al(sb) + al(phb) + al(ab) + 2 * al(ib) + al(stb) + al(rb) + 256);
   if (rc) return rc;
   char* b = (char*)c->io.p;
-  ucl_model_params* p_d = (ucl_model_params*)b;
+  SolveIO io = make_io(c, nmodels, max_rows);
+  io.params = (ucl_model_params*)b;
   b += al(pb);
-  double* s_d = start ? (double*)b : nullptr;
+  io.start = start ? (double*)b : nullptr;
   b += al(sb);
-  double* ph_d = (double*)b;
+  io.phys = (double*)b;
   b += al(phb);
-  double* ab_d = (double*)b;
+  io.abund = (double*)b;
   b += al(ab);
-  int* nr_d = (int*)b;
+  io.nrows = (int*)b;
   b += al(ib);
-  int* fl_d = (int*)b;
+  io.flags = (int*)b;
   b += al(ib);
-  ucl_model_stats* st_d = stats_out ? (ucl_model_stats*)b : nullptr;
+  io.stats = stats_out ? (ucl_model_stats*)b : nullptr;
+  b += al(stb);
+  io.rates = rates_out ? (double*)b : nullptr;
   cudaStream_t s = c->stream;
-  if (cudaMemcpyAsync(p_d, params, pb, cudaMemcpyHostToDevice, s) != cudaSuccess) return UCL_E_CUDA;
-  if (start && cudaMemcpyAsync(s_d, start, sb, cudaMemcpyHostToDevice, s) != cudaSuccess) return UCL_E_CUDA;
-  rc = precision == UCL_PREC_MIXED
-           ? solve_dev<float>(c, nmodels, p_d, s_d, max_rows, ph_d, ab_d, nr_d, fl_d, st_d, 0)
-           : solve_dev<double>(c, nmodels, p_d, s_d, max_rows, ph_d, ab_d, nr_d, fl_d, st_d, 0);
+  if (cudaMemcpyAsync((void*)io.params, params, pb, cudaMemcpyHostToDevice, s) != cudaSuccess) return UCL_E_CUDA;
+  if (start && cudaMemcpyAsync((void*)io.start, start, sb, cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return UCL_E_CUDA;
+  rc = precision == UCL_PREC_MIXED ? solve_dev<float>(c, c->ws, io, 0, s) : solve_dev<double>(c, c->ws, io, 0, s);
   if (rc) return rc;
-  if (cudaMemcpyAsync(phys_out, ph_d, phb, cudaMemcpyDeviceToHost, s) != cudaSuccess) return UCL_E_CUDA;
-  if (cudaMemcpyAsync(abund_out, ab_d, ab, cudaMemcpyDeviceToHost, s) != cudaSuccess) return UCL_E_CUDA;
-  if (cudaMemcpyAsync(nrows_out, nr_d, ib, cudaMemcpyDeviceToHost, s) != cudaSuccess) return UCL_E_CUDA;
-  if (cudaMemcpyAsync(flag_out, fl_d, ib, cudaMemcpyDeviceToHost, s) != cudaSuccess) return UCL_E_CUDA;
-  if (stats_out && cudaMemcpyAsync(stats_out, st_d, stb, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+  if (cudaMemcpyAsync(phys_out, io.phys, phb, cudaMemcpyDeviceToHost, s) != cudaSuccess) return UCL_E_CUDA;
+  if (cudaMemcpyAsync(abund_out, io.abund, ab, cudaMemcpyDeviceToHost, s) != cudaSuccess) return UCL_E_CUDA;
+  if (cudaMemcpyAsync(nrows_out, io.nrows, ib, cudaMemcpyDeviceToHost, s) != cudaSuccess) return UCL_E_CUDA;
+  if (cudaMemcpyAsync(flag_out, io.flags, ib, cudaMemcpyDeviceToHost, s) != cudaSuccess) return UCL_E_CUDA;
+  if (stats_out && cudaMemcpyAsync(stats_out, io.stats, stb, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return UCL_E_CUDA;
+  if (rates_out && cudaMemcpyAsync(rates_out, io.rates, rb, cudaMemcpyDeviceToHost, s) != cudaSuccess)
     return UCL_E_CUDA;
   return cuda_status(cudaStreamSynchronize(s));
 }
 
 // ---------------------------------------------------------------------------
-// single-evaluation entry points (parity probes)
+// single-evaluation entry points (parity probes; the context's first network)
 extern "C" int ucl_rates_batch(ucl_ctx* c, int nsys, const ucl_model_params* params, double* abund, const double* av,
                                double* phi, double* rates) {
   if (!c || nsys < 0 || !params || !abund || !av || !phi || !rates) return UCL_E_ARG;
   if (nsys == 0) return UCL_OK;
   cudaSetDevice(c->device);
-  const int n = c->neq, nr = c->nreac;
+  const DevNet& dn = c->tabs[0].dn;
+  const int n = dn.neq, nr = dn.nreac;
   auto al = [](size_t x) { return (x + 255) / 256 * 256; };
   const size_t pb = sizeof(ucl_model_params) * nsys, yb = (size_t)nsys * n * 8, vb = (size_t)nsys * 8,
                rb = (size_t)nsys * nr * 8;
@@ -896,7 +996,7 @@ extern "C" int ucl_rates_batch(ucl_ctx* c, int nsys, const ucl_model_params* par
   cudaMemcpyAsync(av_d, av, vb, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(phi_d, phi, vb, cudaMemcpyHostToDevice, s);
   const size_t sm = (size_t)(n + nr) * 8;
-  k_rates<<<nsys, NT, sm, s>>>(c->tab.dn, p_d, y_d, av_d, phi_d, r_d, nsys);
+  k_rates<<<nsys, NT, sm, s>>>(dn, p_d, y_d, av_d, phi_d, r_d, nsys);
   if (cudaGetLastError() != cudaSuccess) return UCL_E_CUDA;
   cudaMemcpyAsync(rates, r_d, rb, cudaMemcpyDeviceToHost, s);
   cudaMemcpyAsync(abund, y_d, yb, cudaMemcpyDeviceToHost, s);
@@ -907,11 +1007,13 @@ extern "C" int ucl_rates_batch(ucl_ctx* c, int nsys, const ucl_model_params* par
 static int rhs_jac(ucl_ctx* c, int nsys, const ucl_model_params* params, const double* y, const double* rates,
                    const double* av, double* ydot, double* jac) {
   cudaSetDevice(c->device);
-  const int n = c->neq, nr = c->nreac;
+  const DevNet& dn = c->tabs[0].dn;
+  const int n = dn.neq, nr = dn.nreac;
   auto al = [](size_t x) { return (x + 255) / 256 * 256; };
   const size_t pb = sizeof(ucl_model_params) * nsys, yb = (size_t)nsys * n * 8, vb = (size_t)nsys * 8,
-               rb = (size_t)nsys * nr * 8, jb = jac ? (size_t)nsys * n * n * 8 : 0;
-  int rc = c->small.ensure(al(pb) + 2 * al(yb) + al(vb) + al(rb) + al(jb));
+               rb = (size_t)nsys * nr * 8, jb = jac ? (size_t)nsys * n * n * 8 : 0,
+               jpb = jac ? (size_t)nsys * dn.njch * 8 : 0;
+  int rc = c->small.ensure(al(pb) + 2 * al(yb) + al(vb) + al(rb) + al(jb) + al(jpb));
   if (rc) return rc;
   char* b = (char*)c->small.p;
   ucl_model_params* p_d = (ucl_model_params*)b;
@@ -925,14 +1027,17 @@ static int rhs_jac(ucl_ctx* c, int nsys, const ucl_model_params* params, const d
   double* r_d = (double*)b;
   b += al(rb);
   double* j_d = jac ? (double*)b : nullptr;
+  b += al(jb);
+  double* jp_d = jac ? (double*)b : nullptr;
   cudaStream_t s = c->stream;
   cudaMemcpyAsync(p_d, params, pb, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(y_d, y, yb, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(av_d, av, vb, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(r_d, rates, rb, cudaMemcpyHostToDevice, s);
-  const size_t sm = ((size_t)2 * n + 3 * (size_t)nr + (size_t)c->tab.nchunk + 1024) * 8;
-  cudaFuncSetAttribute(k_rhs_jac, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_rhs_jac<<<nsys, NT, sm, s>>>(c->tab.dn, p_d, y_d, r_d, av_d, yd_d, j_d, nsys);
+  const size_t sm = ((size_t)2 * n + 3 * (size_t)nr + (size_t)dn.nchunk + JAC_VEC_DOUBLES) * 8;
+  if (cudaFuncSetAttribute(k_rhs_jac, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+    return UCL_E_UNSUPPORTED;
+  k_rhs_jac<<<nsys, NT, sm, s>>>(dn, p_d, y_d, r_d, av_d, yd_d, j_d, jp_d, nsys);
   if (cudaGetLastError() != cudaSuccess) return UCL_E_CUDA;
   if (ydot) cudaMemcpyAsync(ydot, yd_d, yb, cudaMemcpyDeviceToHost, s);
   if (jac) cudaMemcpyAsync(jac, j_d, jb, cudaMemcpyDeviceToHost, s);
@@ -957,21 +1062,186 @@ extern "C" int ucl_serve_models_device(ucl_ctx* c, int nmodels, const ucl_model_
                                        const double* arrival_d, const double* start_d, int max_rows, double* phys_d,
                                        double* abund_d, int* nrows_d, int* flags_d, ucl_model_stats* stats_d,
                                        int precision, int max_ctas, void* stream) {
-  if (!c || nmodels < 0 || max_rows < 1 || !params_d || !arrival_d || !phys_d || !abund_d || !nrows_d || !flags_d)
-    return UCL_E_ARG;
-  if (precision != UCL_PREC_FP64 && precision != UCL_PREC_MIXED) return UCL_E_ARG;
+  int rc = check_solve_args(c, nmodels, max_rows, params_d, phys_d, abund_d, nrows_d, flags_d, precision);
+  if (rc) return rc;
+  if (!arrival_d) return UCL_E_ARG;
   if (nmodels == 0) return UCL_OK;
+  SolveIO io = make_io(c, nmodels, max_rows);
+  io.params = params_d; io.start = start_d; io.phys = phys_d; io.abund = abund_d;
+  io.nrows = nrows_d; io.flags = flags_d; io.stats = stats_d;
+  return solve_device(c, io, precision, max_ctas, stream, arrival_d);
+}
+
+// ---------------------------------------------------------------------------
+// Live serving session: a persistent solver fed through a request ring in
+// pinned, device-mapped host memory (LiveQueue in ucl_model.cuh).
+struct ucl_server {
+  ucl_ctx* c = nullptr;
+  int cap = 0, max_rows = 0, precision = 0;
+  cudaStream_t kstream = nullptr, cstream = nullptr;
+  DevBuf ws, out;
+  double *phys = nullptr, *abund = nullptr;
+  int *nrows = nullptr, *flags = nullptr;
+  ucl_model_stats* stats = nullptr;
+  // pinned host memory (and its device aliases)
+  ucl_model_params* req_h = nullptr;
+  unsigned* ctl_h = nullptr;  // [0] tail, [1] closed, [2..] done[cap]
+  int* status_h = nullptr;
+  ucl_model_params* req_d = nullptr;
+  unsigned* ctl_d = nullptr;
+  int* status_d = nullptr;
+  std::mutex mu;
+  long long next = 0;              // number of the next request
+  std::vector<long long> rec_req;  // request held by each record, -1 free
+  bool closed = false;
+};
+
+static void server_free(ucl_server* s) {
+  if (s->kstream) cudaStreamDestroy(s->kstream);
+  if (s->cstream) cudaStreamDestroy(s->cstream);
+  s->ws.release();
+  s->out.release();
+  if (s->req_h) cudaFreeHost(s->req_h);
+  if (s->ctl_h) cudaFreeHost(s->ctl_h);
+  if (s->status_h) cudaFreeHost(s->status_h);
+  delete s;
+}
+
+extern "C" int ucl_server_open(ucl_ctx* c, int capacity, int max_rows, int precision, int max_ctas,
+                               double idle_timeout_s, ucl_server** out) {
+  if (!c || !out || capacity < 0 || max_rows < 1 || !(idle_timeout_s >= 0.0)) return UCL_E_ARG;
+  if (idle_timeout_s == 0.0) idle_timeout_s = 1200.0;
+  if (idle_timeout_s > 80000.0) return UCL_E_ARG;  // the sleep count must fit 32 bits
+  if (precision != UCL_PREC_FP64 && precision != UCL_PREC_MIXED) return UCL_E_ARG;
   cudaSetDevice(c->device);
-  cudaStream_t user = (cudaStream_t)stream;
-  cudaStream_t keep = c->stream;
-  if (user) c->stream = user;
-  const int rc = precision == UCL_PREC_MIXED
-                     ? solve_dev<float>(c, nmodels, params_d, start_d, max_rows, phys_d, abund_d, nrows_d, flags_d,
-                                        stats_d, max_ctas, arrival_d)
-                     : solve_dev<double>(c, nmodels, params_d, start_d, max_rows, phys_d, abund_d, nrows_d, flags_d,
-                                         stats_d, max_ctas, arrival_d);
-  c->stream = keep;
-  return rc;
+  auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+  const size_t rec = al((size_t)max_rows * UCL_N_PHYS * 8) + al((size_t)max_rows * c->nspec * 8);
+  const size_t per_rec = rec + 2 * 4 + sizeof(ucl_model_stats);
+  if (capacity == 0) {  // as many output records as the context's HBM budget holds
+    capacity = (int)std::min<size_t>(1 << 20, c->budget / per_rec);
+    if (capacity < 1) return UCL_E_NOMEM;
+  }
+  ucl_server* s = new ucl_server();
+  s->c = c;
+  s->cap = capacity;
+  s->max_rows = max_rows;
+  s->precision = precision;
+  s->rec_req.assign(capacity, -1);
+  const size_t cap = (size_t)capacity;
+  const size_t phb = al(cap * max_rows * UCL_N_PHYS * 8), abb = al(cap * max_rows * c->nspec * 8),
+               ib = al(cap * 4), stb = al(cap * sizeof(ucl_model_stats));
+  if (s->out.ensure(phb + abb + 2 * ib + stb) != UCL_OK) { server_free(s); return UCL_E_NOMEM; }
+  char* b = (char*)s->out.p;
+  s->phys = (double*)b;
+  s->abund = (double*)(b + phb);
+  s->nrows = (int*)(b + phb + abb);
+  s->flags = (int*)(b + phb + abb + ib);
+  s->stats = (ucl_model_stats*)(b + phb + abb + 2 * ib);
+  if (cudaHostAlloc((void**)&s->req_h, cap * sizeof(ucl_model_params), cudaHostAllocMapped) != cudaSuccess ||
+      cudaHostAlloc((void**)&s->ctl_h, (cap + 2) * sizeof(unsigned), cudaHostAllocMapped) != cudaSuccess ||
+      cudaHostAlloc((void**)&s->status_h, sizeof(int), cudaHostAllocMapped) != cudaSuccess) {
+    server_free(s);
+    return UCL_E_NOMEM;
+  }
+  memset(s->ctl_h, 0, (cap + 2) * sizeof(unsigned));
+  *s->status_h = 0;
+  if (cudaHostGetDevicePointer((void**)&s->req_d, s->req_h, 0) != cudaSuccess ||
+      cudaHostGetDevicePointer((void**)&s->ctl_d, s->ctl_h, 0) != cudaSuccess ||
+      cudaHostGetDevicePointer((void**)&s->status_d, s->status_h, 0) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&s->kstream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&s->cstream, cudaStreamNonBlocking) != cudaSuccess) {
+    server_free(s);
+    return UCL_E_CUDA;
+  }
+  SolveIO io = make_io(c, capacity, max_rows);
+  io.params = s->req_d;
+  io.phys = s->phys; io.abund = s->abund; io.nrows = s->nrows; io.flags = s->flags; io.stats = s->stats;
+  LiveQueue q;
+  q.req = s->req_d;
+  q.tail = s->ctl_d;
+  q.closed = s->ctl_d + 1;
+  q.done = s->ctl_d + 2;
+  q.status = s->status_d;
+  q.cap = capacity;
+  q.idle_limit = (unsigned)(idle_timeout_s / 20e-6) + 1u;
+  const int rc = precision == UCL_PREC_MIXED ? solve_dev<float>(c, s->ws, io, max_ctas, s->kstream, nullptr, q)
+                                             : solve_dev<double>(c, s->ws, io, max_ctas, s->kstream, nullptr, q);
+  if (rc) { server_free(s); return rc; }
+  *out = s;
+  return UCL_OK;
+}
+
+extern "C" int ucl_server_capacity(const ucl_server* s) { return s ? s->cap : 0; }
+
+extern "C" int ucl_server_submit(ucl_server* s, const ucl_model_params* params, long long* request) {
+  if (!s || !params || !request) return UCL_E_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->closed) return UCL_E_ARG;
+  const long long k = s->next;
+  const int r = (int)(k % s->cap);
+  if (s->rec_req[r] != -1) return UCL_E_AGAIN;  // record still holds an untaken request
+  s->req_h[r] = *params;
+  s->rec_req[r] = k;
+  s->next = k + 1;
+  __atomic_store_n(&s->ctl_h[0], (unsigned)(k + 1), __ATOMIC_RELEASE);
+  *request = k;
+  return UCL_OK;
+}
+
+// 1 when request k's outputs are complete, 0 while it is pending
+extern "C" int ucl_server_poll(ucl_server* s, long long k) {
+  if (!s || k < 0) return UCL_E_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  const int r = (int)(k % s->cap);
+  if (k >= s->next || s->rec_req[r] != k) return UCL_E_ARG;
+  if (__atomic_load_n(&s->ctl_h[2 + r], __ATOMIC_ACQUIRE) == (unsigned)(k + 1)) return 1;
+  if (__atomic_load_n(s->status_h, __ATOMIC_ACQUIRE) != 0) return UCL_E_TIMEOUT;
+  const cudaError_t e = cudaStreamQuery(s->kstream);
+  if (e == cudaSuccess) {  // the solver has ended: the request was lost with it
+    if (__atomic_load_n(&s->ctl_h[2 + r], __ATOMIC_ACQUIRE) == (unsigned)(k + 1)) return 1;
+    return UCL_E_TIMEOUT;
+  }
+  if (e != cudaErrorNotReady) return UCL_E_CUDA;
+  return 0;
+}
+
+extern "C" int ucl_server_take(ucl_server* s, long long k, double* phys_out, double* abund_out, int* nrows_out,
+                               int* flag_out, ucl_model_stats* stats_out) {
+  if (!s || !phys_out || !abund_out || !nrows_out || !flag_out) return UCL_E_ARG;
+  const int p = ucl_server_poll(s, k);
+  if (p < 0) return p;
+  if (p == 0) return UCL_E_AGAIN;
+  cudaSetDevice(s->c->device);
+  const int r = (int)(k % s->cap), R = s->max_rows, ns = s->c->nspec;
+  cudaStream_t st = s->cstream;
+  if (cudaMemcpyAsync(phys_out, s->phys + (size_t)r * R * UCL_N_PHYS, (size_t)R * UCL_N_PHYS * 8,
+                      cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(abund_out, s->abund + (size_t)r * R * ns, (size_t)R * ns * 8, cudaMemcpyDeviceToHost, st) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(nrows_out, s->nrows + r, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(flag_out, s->flags + r, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      (stats_out && cudaMemcpyAsync(stats_out, s->stats + r, sizeof(ucl_model_stats), cudaMemcpyDeviceToHost,
+                                    st) != cudaSuccess))
+    return UCL_E_CUDA;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return UCL_E_CUDA;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->rec_req[r] = -1;
+  return UCL_OK;
+}
+
+extern "C" int ucl_server_close(ucl_server* s) {
+  if (!s) return UCL_E_ARG;
+  cudaSetDevice(s->c->device);
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->closed = true;
+    __atomic_store_n(&s->ctl_h[1], 1u, __ATOMIC_RELEASE);
+  }
+  const cudaError_t e = cudaStreamSynchronize(s->kstream);
+  const int status = *s->status_h;
+  server_free(s);
+  if (e != cudaSuccess) return UCL_E_CUDA;
+  return status ? status : UCL_OK;
 }
 
 // batched LU of row-major n x n matrices already on the device
@@ -991,6 +1261,7 @@ extern "C" int ucl_lu_factor_device(ucl_ctx* c, int nsys, int n, int precision, 
                                     int* info_dev, void* stream) {
   if (!c || nsys < 0 || n < 2 || n > MAX_NEQ || (n % 4) != 0 || !mats_dev || !perm_dev || !info_dev)
     return UCL_E_ARG;
+  if (precision != UCL_PREC_FP64 && precision != UCL_PREC_MIXED) return UCL_E_ARG;
   if (((uintptr_t)mats_dev & 15) != 0) return UCL_E_ARG;
   if (nsys == 0) return UCL_OK;
   cudaSetDevice(c->device);
@@ -1002,26 +1273,36 @@ extern "C" int ucl_lu_factor_device(ucl_ctx* c, int nsys, int n, int precision, 
 // ---------------------------------------------------------------------------
 // Allocation-free batched LU.  The row-interchange scratch lives in a fixed
 // file-scope device array; the kernel's grid is capped so that every CTA has
-// its own part of it.  Set-up (symbol address, shared-memory attributes) is
-// done once per device by the first call on that device.
+// its own part of it and every CTA is resident at once.  Set-up (symbol
+// address, shared-memory attributes, SM count) is done once per device by
+// the first call on that device; a set-up that fails is tried again by the
+// next call.
 static __device__ __align__(256) unsigned char g_lu_scratch[UCL_LU_STATIC_SCRATCH_BYTES];
 
 namespace {
 struct StaticLuDev {
-  std::once_flag once;
-  int rc = UCL_E_CUDA;
+  bool ready = false;
   void* scratch = nullptr;
+  int nsm = 0;
 };
+std::mutex g_static_lu_mu;
 StaticLuDev g_static_lu[64];
 }  // namespace
 
 template <typename T>
-static int lu_static(int nsys, int n, void* mats, int* perm, int* info, void* scratch, cudaStream_t st) {
+static int lu_static(int nsys, int n, void* mats, int* perm, int* info, const StaticLuDev& S, cudaStream_t st) {
   const size_t per = (size_t)2 * LuCfg<T>::NB * n * sizeof(T);
   const int cap = (int)(UCL_LU_STATIC_SCRATCH_BYTES / per);
   if (cap < 1) return UCL_E_ARG;
-  const int grid = std::min(nsys, cap);
-  k_lu_batch_strided<T><<<grid, NT, lu_smem_bytes<T>(n), st>>>((T*)mats, n, perm, info, (T*)scratch, nsys);
+  const size_t sm = lu_smem_bytes<T>(n);
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lu_batch_strided<T>, NT, sm) != cudaSuccess ||
+      per_sm < 1)
+    return UCL_E_CUDA;
+  // no more CTAs than fit on the GPU at once: a CTA beyond that would wait
+  // for a second wave while keeping its whole stride of matrices
+  const int grid = std::min(std::min(nsys, cap), per_sm * S.nsm);
+  k_lu_batch_strided<T><<<grid, NT, sm, st>>>((T*)mats, n, perm, info, (T*)S.scratch, nsys);
   return cuda_status(cudaGetLastError());
 }
 
@@ -1034,23 +1315,28 @@ extern "C" int ucl_lu_factor_device_static(int nsys, int n, int precision, void*
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return UCL_E_CUDA;
   StaticLuDev& S = g_static_lu[dev];
-  std::call_once(S.once, [&S]() {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_lu_scratch) != cudaSuccess) return;
-    const int sm32 = (int)std::max(lu_smem_bytes<float>(MAX_NEQ), lu_smem_bytes<float>(TC_MAX_N));
-    const int sm64 = (int)lu_smem_bytes<double>(MAX_NEQ);
-    if (cudaFuncSetAttribute(k_lu_batch_strided<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32) !=
-            cudaSuccess ||
-        cudaFuncSetAttribute(k_lu_batch_strided<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm64) !=
-            cudaSuccess)
-      return;
-    S.scratch = p;
-    S.rc = UCL_OK;
-  });
-  if (S.rc != UCL_OK) return S.rc;
-  cudaStream_t st = (cudaStream_t)stream;
-  return precision == UCL_PREC_MIXED ? lu_static<float>(nsys, n, mats_dev, perm_dev, info_dev, S.scratch, st)
-                                     : lu_static<double>(nsys, n, mats_dev, perm_dev, info_dev, S.scratch, st);
+  {
+    std::lock_guard<std::mutex> lk(g_static_lu_mu);
+    if (!S.ready) {
+      void* p = nullptr;
+      int nsm = 0;
+      if (cudaGetSymbolAddress(&p, g_lu_scratch) != cudaSuccess) return UCL_E_CUDA;
+      const int sm32 = (int)std::max(lu_smem_bytes<float>(MAX_NEQ), lu_smem_bytes<float>(TC_MAX_N));
+      const int sm64 = (int)lu_smem_bytes<double>(MAX_NEQ);
+      if (cudaFuncSetAttribute(k_lu_batch_strided<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32) !=
+              cudaSuccess ||
+          cudaFuncSetAttribute(k_lu_batch_strided<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm64) !=
+              cudaSuccess ||
+          cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1)
+        return UCL_E_CUDA;
+      S.scratch = p;
+      S.nsm = nsm;
+      S.ready = true;
+    }
+  }
+  cudaStream_t st = (cudaStream_t)stream;  // NULL: the legacy default stream (there is no context)
+  return precision == UCL_PREC_MIXED ? lu_static<float>(nsys, n, mats_dev, perm_dev, info_dev, S, st)
+                                     : lu_static<double>(nsys, n, mats_dev, perm_dev, info_dev, S, st);
 }
 
 // capacity query used by the host front end
@@ -1058,3 +1344,6 @@ extern "C" int ucl_ctx_slots(const ucl_ctx* c, int precision) {
   if (!c) return 0;
   return precision == UCL_PREC_MIXED ? c->slots_fp32 : c->slots_fp64;
 }
+
+extern "C" int ucl_ctx_nspec(const ucl_ctx* c) { return c ? c->nspec : 0; }
+extern "C" int ucl_ctx_nreac(const ucl_ctx* c) { return c ? c->nreac : 0; }

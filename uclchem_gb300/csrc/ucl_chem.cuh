@@ -19,6 +19,7 @@ struct SysPhys {
   double sm, sb, blr;               // safeMantle, safeBulk, bulkLayersReciprocal at interval start
   double h2col, cocol, ccol;        // column densities at interval start
   double avt, rf, scat1000;         // Av/1.086, radfield/1.7, dust scattering at 1000 A
+  double h2crp;                     // h2CRPRate of the interval (improvedH2CRPDissociation)
 };
 
 // per-interval constants of the photo rates (Av and radfield are fixed over
@@ -253,7 +254,12 @@ __device__ void dev_rates(const DevNet& N, const ucl_model_params& P, SysPhys& S
     const double a = N.alpha[j], b = N.beta[j], g = N.gama[j];
     double r = 0.0;
     switch (t) {
-      case RT_CRP: r = a * P.zeta; break;
+      case RT_CRP:
+        r = a * P.zeta;
+        // improvedH2CRPDissociation overwrites the H2 CR dissociation right
+        // after the CRP block (rates.f90:38-41)
+        if (P.improvedH2CRPDissociation && j == N.rx_h2crp) r = S.h2crp;
+        break;
       case RT_PHOTON:
         r = a * exp(-g * av) * P.radfield / (double)1.7f;
         if (N.iceflag[j] == 2) r = r * icefac_b;
@@ -375,6 +381,7 @@ __device__ void dev_rates(const DevNet& N, const ucl_model_params& P, SysPhys& S
     if (j == N.rx_h2hv) r = h2_photo(S.h2col, P.radfield, av);
     if (j == N.rx_cohv) r = co_photo(S.h2col, S.cocol, P.radfield, av);
     if (j == N.rx_chv) r = c_ionization(N.alpha[j], N.gama[j], T, S.ccol, S.h2col, av, P.radfield);
+    // (rx_* are -1 in a network without these reactions: never matched)
     rate[j] = r;
   }
   __syncthreads();
@@ -432,6 +439,7 @@ __device__ void dev_rhs(const DevNet& N, const ucl_model_params& P, const SysPhy
   const double D = R.D;
   const double h2col = 0.5 * y[N.nh2] * D * S.cs;
   if (warp == 0) {
+    if (N.rx_cohv >= 0) {  // warp-uniform
     const double cocol = 0.5 * y[N.nco] * D * S.cs;
     const double k = co_photo_w(h2col, cocol, S);
     double d1 = 0.0, d2 = 0.0;
@@ -442,8 +450,9 @@ __device__ void dev_rhs(const DevNet& N, const ucl_model_params& P, const SysPhy
       d2 = (co_photo_w(h2col, cocol + dc, S) - k) / dc;
     }
     if (lane == 0) { R.kco = k; R.dkco_dnh2 = d1; R.dkco_dnco = d2; }
+    }
   } else if (warp == 1) {
-    if (lane == 0) {
+    if (lane == 0 && N.rx_h2hv >= 0) {
       R.kh2 = h2_photo_s(h2col, S);
       if (jac_scalars) {
         const double dh = h2col * 1e-6 + 1e-30;
@@ -477,12 +486,12 @@ __device__ void dev_rhs(const DevNet& N, const ucl_model_params& P, const SysPhy
   __syncthreads();
   // photo fluxes, totalSwap and the surface-swap fluxes (warp 0)
   if (warp == 0) {
-    if (lane == 0) {
+    if (lane == 0 && N.rx_h2hv >= 0)
       flux[N.rx_h2hv] = flux_of(N.fshape[N.rx_h2hv], R.kh2, D, y[N.fya[N.rx_h2hv]],
                                 N.fyb[N.rx_h2hv] >= 0 ? y[N.fyb[N.rx_h2hv]] : 0.0, R);
+    if (lane == 0 && N.rx_cohv >= 0)
       flux[N.rx_cohv] = flux_of(N.fshape[N.rx_cohv], R.kco, D, y[N.fya[N.rx_cohv]],
                                 N.fyb[N.rx_cohv] >= 0 ? y[N.fyb[N.rx_cohv]] : 0.0, R);
-    }
     double s = 0.0;
     for (int r = N.swap_lo + lane; r < N.swap_hi; r += 32) s += flux[r];
     s = warp_sum(s);
@@ -555,6 +564,14 @@ __device__ void dev_rhs(const DevNet& N, const ucl_model_params& P, const SysPhy
       R.neg = neg;
       R.sc = sc;
     }
+  } else if (warp == 1 && P.enforceChargeConservation && N.n_ion > 0) {
+    // enforceChargeConservation: the electron derivative is the sum of the
+    // positive ions' (chemistry.f90:333-335); ions are gas-phase species, so
+    // this is independent of warp 0's ice transfer
+    double s = 0.0;
+    for (int k = lane; k < N.n_ion; k += 32) s += ydot[N.ion_list[k]];
+    s = warp_sum(s);
+    if (lane == 0) ydot[N.nelec] = s;
   }
   __syncthreads();
 }
@@ -789,6 +806,18 @@ __device__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhy
     J[(size_t)(N.nbulk) * n + j] = (T)bsum;
   }
   __syncthreads();
+  if (P.enforceChargeConservation && N.n_ion > 0) {
+    // electron row = sum of the ion rows (F sets ydot(nelec) to the ions' sum)
+    for (int j = tid; j < n; j += NT) {
+      double s = 0.0;
+      for (int k = 0; k < N.n_ion; ++k) {
+        const int r = N.ion_list[k];
+        s += (double)J[(size_t)r * n + j] * (SCALED ? wi[r] : 1.0);
+      }
+      J[(size_t)(N.nelec) * n + j] = (T)(SCALED ? s * w[N.nelec] : s);
+    }
+    __syncthreads();
+  }
   if (tid == 0) {
     double dd = 0.0;
     if (P.freefall && D < P.finalDens) {

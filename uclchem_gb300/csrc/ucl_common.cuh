@@ -21,6 +21,10 @@ constexpr int NT = UCL_NT;       // threads per CTA of the solver kernels
 constexpr int NWARP = NT / 32;
 constexpr int MAX_NEQ = 520;     // largest NEQ the kernels are compiled for
 constexpr int LMAXP = 7;         // Nordsieck columns held (MAXORD+2)
+// doubles of the Jacobian's vector scratch: [0, 256) per-row/ice
+// coefficients, [256, 512) their scaled copies, [512, 512 + NEQ) one staged
+// matrix row
+constexpr int JAC_VEC_DOUBLES = 512 + MAX_NEQ + 8;
 
 // Reaction types (the block of calculateReactionRates that last writes the
 // reaction's rate; rates.f90:33-342).
@@ -52,8 +56,15 @@ struct DevNet {
   // named species (0-based; absent elements point at the density slot)
   int nh, nh2, nhe, nc, ncx, nco, nelec, nsurf, nbulk, nmgx, nsix, nsx, nclx, no, nn, nmg, np,
       nf, nna, nli, npah, nd, n18o, n15n, n13c;
-  // named reactions
-  int rx_h2hv, rx_cohv, rx_chv;
+  // named reactions (-1 where the network has none: a generic network has
+  // no self-shielded photo reactions)
+  int rx_h2hv, rx_cohv, rx_chv, rx_h2crp;
+  // positive ions (species names containing '+'), for enforceChargeConservation
+  int n_ion;
+  const int* ion_list;
+  // refractory ice species subtracted from safeBulk at interval start
+  int n_refr;
+  const int* refr_list;
   // ---- rates ----
   const uint8_t* rtype;
   const uint8_t* iceflag;  // PHOTON/CRPHOT: 1 surface, 2 bulk reactant; LHDES/ERDES: 1 bulk reactant
@@ -111,8 +122,9 @@ struct DevNet {
   const int* je_end;
   const int* jc_key;
   const float* jc_coef;
-  int njch;                // chunks of <= 8 contributions
-  int npart;               // max(nchunk, njch): partial-sum scratch per system
+  int njch;                // chunks of <= 8 contributions (their partial sums
+                           // go to a per-slot global buffer of njch doubles)
+  int npart;               // max(nchunk, njch)
   const unsigned* jent;    // nchunks << 16 | first chunk
   const unsigned* jchunk;  // len << 16 | first contribution
   const unsigned* jcpack;  // (coef & 0xff) << 16 | key

@@ -29,6 +29,25 @@ __device__ double target_time(double ty, double spy) {
   return spy * 1.0e-7;
 }
 
+// Inputs and outputs of a batched solve.  Per-model arrays use the strides
+// of the context's largest network, so models of different networks can
+// share one launch: model i's start vector is start[i*start_stride ...],
+// its rows abund[(i*max_rows + r)*ab_stride ...] and
+// rates[(i*max_rows + r)*rate_stride ...].
+struct SolveIO {
+  const ucl_model_params* params;
+  const double* start;       // nullptr: elemental start of initializeChemistry
+  double* phys;
+  double* abund;
+  double* rates;             // nullptr: no rates rows
+  int* nrows;
+  int* flags;
+  ucl_model_stats* stats;    // may be nullptr
+  int nmodels, max_rows, start_stride, ab_stride, rate_stride;
+  const DevNet* nets;        // device array of the context's networks
+  const int* net_of;         // network of each model (nullptr: all network 0)
+};
+
 // start-of-interval quantities of updateChemistry (chemistry.f90:166-200)
 template <typename T>
 __device__ void interval_start(Ctx<T>& C, bool refresh_density) {
@@ -44,10 +63,17 @@ __device__ void interval_start(Ctx<T>& C, bool refresh_density) {
     double sb = 0.0, ss = 0.0;
     for (int i = 0; i < N.n_bulk; i++) sb = i == 0 ? y[N.bulk_list[i]] : sb + y[N.bulk_list[i]];
     for (int i = 0; i < N.n_surface; i++) ss = i == 0 ? y[N.surface_list[i]] : ss + y[N.surface_list[i]];
-    y[N.nbulk] = sb;
-    y[N.nsurf] = ss;
+    // (a network without ices has no SURFACE/BULK totals: its nsurf/nbulk
+    // name the density slot, which must not be overwritten)
+    if (N.n_bulk > 0) y[N.nbulk] = sb;
+    if (N.n_surface > 0) y[N.nsurf] = ss;
     S.sm = fmax(1e-30, ss);
     S.sb = fmax(1e-30, sb);
+    if (N.n_refr > 0) {  // refractory ices do not count as bulk (chemistry.f90:196)
+      double r = 0.0;
+      for (int i = 0; i < N.n_refr; i++) r += y[N.refr_list[i]];
+      S.sb = S.sb - r;
+    }
     const double q = cK.NUM_SITES_PER_GRAIN / (cK.GAS_DUST_DENSITY_RATIO * S.sb);
     S.blr = q < 1.0 ? q : 1.0;
     photo_setup(S, sh.P.radfield);
@@ -55,15 +81,61 @@ __device__ void interval_start(Ctx<T>& C, bool refresh_density) {
   __syncthreads();
 }
 
+// x**k for an integer k >= 0 by the right-to-left binary method (Knuth,
+// TAOCP 4.6.3): square x while halving k, multiplying the squares of the set
+// bits into the result, the way compiled Fortran evaluates a real raised to
+// a variable integer power.
+__device__ __forceinline__ double ipow_bin(double x, int k) {
+  unsigned e = (unsigned)k;
+  double r = (e & 1u) ? x : 1.0;
+  while (e >>= 1) {
+    x = x * x;
+    if (e & 1u) r = r * x;
+  }
+  return r;
+}
+
+// H2 cosmic-ray dissociation rate of ionizationDependency
+// (physics-core.f90:121-157): 10^(sum_k c_k log10(N)^k) * zeta, with N the
+// parcel's column density and c_k the L or H model coefficients of
+// physics-core.f90:29-37 (Padovani et al. 2018b fits; data).
+__device__ double h2_crp_rate(const ucl_model_params& P, double coldens) {
+  const double cL[10] = {1.582911005330e7, -6.465722684896e6, 1.172189025424e6, -1.237950798073e5,
+                         8.393404654312e3, -3.788811358130e2, 1.138688455029e1,  -2.197136304567e-1,
+                         2.469841278950e-3, -1.232393620924e-5};
+  const double cH[10] = {1.217227462831e7, -4.989649250304e6, 9.079152156645e5, -9.624890825395e4,
+                         6.551161486120e3, -2.968976216187e2, 8.959037875226e0,  -1.735757324445e-1,
+                         1.959267277734e-3, -9.816996707980e-6};
+  const double* c = P.ionModel == 'H' ? cH : cL;
+  const double x = log10(coldens);
+  double s = 0.0;
+  for (int k = 0; k < 10; ++k) s = s + c[k] * ipow_bin(x, k);
+  return pow(10.0, s) * P.zeta;
+}
+
+// One output row (io.f90:74-93).  With rates_out, the row of the rates
+// array too: the reference's rate() as it stands at output time, i.e. the
+// interval's calculateReactionRates values with the H2 and CO
+// photodissociation entries as the last F evaluation left them
+// (chemistry.f90:315-318); all zero before the first interval.
 template <typename T>
-__device__ void write_row(Ctx<T>& C, int mi, int max_rows, double* phys_out, double* abund_out) {
+__device__ void write_row(Ctx<T>& C, const SolveIO& io, int mi) {
   Shared& sh = *C.sh;
-  const int nspec = C.N->nspec;
+  const DevNet& N = *C.N;
+  const int nspec = N.nspec, max_rows = io.max_rows;
   const int row = sh.ms.row;
-  double* ab = abund_out + ((size_t)mi * max_rows + row) * nspec;
+  double* ab = io.abund + ((size_t)mi * max_rows + row) * io.ab_stride;
   for (int i = threadIdx.x; i < nspec; i += NT) ab[i] = C.y[i];
+  if (io.rates) {
+    double* rr = io.rates + ((size_t)mi * max_rows + row) * io.rate_stride;
+    for (int j = threadIdx.x; j < N.nreac; j += NT) {
+      double v = 0.0;
+      if (row > 0) v = j == N.rx_h2hv ? sh.R.kh2 : j == N.rx_cohv ? sh.R.kco : C.W.rate[j];
+      rr[j] = v;
+    }
+  }
   if (threadIdx.x == 0) {
-    double* ph = phys_out + ((size_t)mi * max_rows + row) * UCL_N_PHYS;
+    double* ph = io.phys + ((size_t)mi * max_rows + row) * UCL_N_PHYS;
     ph[0] = sh.ms.tyears;
     ph[1] = sh.S.dens;
     ph[2] = sh.S.T;
@@ -78,9 +150,8 @@ __device__ void write_row(Ctx<T>& C, int mi, int max_rows, double* phys_out, dou
 }
 
 template <typename T>
-__device__ void run_model(Ctx<T>& C, const ucl_model_params* params, const double* start, int mi, int max_rows,
-                          double* phys_out, double* abund_out, int* nrows_out, int* flag_out,
-                          ucl_model_stats* stats) {
+__device__ void run_model(Ctx<T>& C, const SolveIO& io, int mi) {
+  const int max_rows = io.max_rows;
   Shared& sh = *C.sh;
   ModelState& ms = sh.ms;
   SysPhys& S = sh.S;
@@ -88,7 +159,7 @@ __device__ void run_model(Ctx<T>& C, const ucl_model_params* params, const doubl
   const int tid = threadIdx.x, n = C.n;
   double* y = C.y;
   if (tid == 0) {
-    sh.P = params[mi];
+    sh.P = io.params[mi];
     const ucl_model_params& P = sh.P;
     ms.t0 = globaltimer_ns();
     const double cloudSize = (P.rout - P.rin) * cK.PC;
@@ -99,6 +170,7 @@ __device__ void run_model(Ctx<T>& C, const ucl_model_params* params, const doubl
     S.av = P.baseAv + ms.coldens / 1.6e21;
     S.dens = P.freefall ? (double)1.001f * P.initialDens : P.initialDens;
     S.phi = P.phi;
+    S.h2crp = 0.0;  // h2CRPRate before the first physics update: a fresh process's zero
     ms.t = 0.0;
     ms.tyears = 0.0;
     ms.flag = 0;
@@ -109,15 +181,22 @@ __device__ void run_model(Ctx<T>& C, const ucl_model_params* params, const doubl
     ms.nst = ms.nfe = ms.nje = ms.nlu = ms.nni = ms.ncfn = ms.netf = 0;
     for (int k = 0; k < 5; k++) ms.tacc[k] = 0;
     sh.d.mxstep = P.mxstep;
-    if (P.points != 1 || P.improvedH2CRPDissociation || P.enforceChargeConservation) ms.flag = UCL_PHYSICS_INIT_ERROR;
+    // coreInitializePhysics's checks (physics-core.f90:55-64) give
+    // PHYSICS_INIT_ERROR; so does points > 1: coreUpdatePhysics reads
+    // coldens(dstep-1) = coldens(0), outside coldens(1:points), for the first
+    // parcel (physics-core.f90:80), so the reference's multi-parcel result is
+    // undefined and the parcels share one retried targetTime
+    if (P.points != 1 || (P.ionModel != 'L' && P.ionModel != 'H') ||
+        (P.improvedH2CRPDissociation && !P.cosmicRayAttenuation))
+      ms.flag = UCL_PHYSICS_INIT_ERROR;
   }
   __syncthreads();
   const ucl_model_params& P = sh.P;
   // initial abundances (initializeChemistry, chemistry.f90:57-105)
   for (int i = tid; i < n; i += NT) y[i] = 1.0e-30;
   __syncthreads();
-  if (start) {
-    for (int i = tid; i < n; i += NT) y[i] = start[(size_t)mi * n + i];
+  if (io.start) {
+    for (int i = tid; i < n; i += NT) y[i] = io.start[(size_t)mi * io.start_stride + i];
   } else {
     if (tid == 0) {
       y[N.no] = P.fo; y[N.nn] = P.fn; y[N.nmg] = P.fmg; y[N.np] = P.fp; y[N.nf] = P.ff;
@@ -141,7 +220,7 @@ __device__ void run_model(Ctx<T>& C, const ucl_model_params* params, const doubl
     }
   }
   __syncthreads();
-  if (ms.flag == 0) write_row(C, mi, max_rows, phys_out, abund_out);
+  if (ms.flag == 0) write_row(C, io, mi);
   for (;;) {
     if (tid == 0)
       ms.go = (ms.flag == 0) && ((P.endAtFinalDensity && S.dens < P.finalDens) ||
@@ -186,6 +265,14 @@ __device__ void run_model(Ctx<T>& C, const ucl_model_params* params, const doubl
       }
       __syncthreads();
       if (ms.flag < 0) break;
+      if (P.enforceChargeConservation && tid == 0) {
+        // electrons = sum of the positive ions after every DVODE call
+        // (integrateODESystem, chemistry.f90:287-291)
+        double e = 0.0;
+        for (int k = 0; k < N.n_ion; ++k) e += y[N.ion_list[k]];
+        if (N.n_ion > 0) y[N.nelec] = e;
+      }
+      __syncthreads();
       for (int i = tid; i < n; i += NT)
         if (y[i] < 1.0e-30) y[i] = 1.0e-30;
       __syncthreads();
@@ -206,17 +293,18 @@ __device__ void run_model(Ctx<T>& C, const ucl_model_params* params, const doubl
         ms.coldens = S.cs * S.dens;  // coreUpdatePhysics (physics-core.f90:75-88)
         S.av = P.baseAv + ms.coldens / 1.6e21;
         S.Td = S.T;
+        if (P.cosmicRayAttenuation && P.improvedH2CRPDissociation) S.h2crp = h2_crp_rate(P, ms.coldens);
         if (ms.row >= max_rows) ms.flag = UCL_NOT_ENOUGH_TIMEPOINTS_ERROR;
       }
     }
     __syncthreads();
     if (ms.flag < 0) break;
-    write_row(C, mi, max_rows, phys_out, abund_out);
+    write_row(C, io, mi);
   }
   if (tid == 0) {
-    nrows_out[mi] = ms.row;
-    flag_out[mi] = ms.flag;
-    if (stats) {
+    io.nrows[mi] = ms.row;
+    io.flags[mi] = ms.flag;
+    if (io.stats) {
       ucl_model_stats st;
       st.nst = ms.nst; st.nfe = ms.nfe; st.nje = ms.nje; st.nlu = ms.nlu; st.nni = ms.nni;
       st.ncfn = ms.ncfn; st.netf = ms.netf;
@@ -231,7 +319,7 @@ __device__ void run_model(Ctx<T>& C, const ucl_model_params* params, const doubl
       const unsigned long long t1 = globaltimer_ns();
       st.queue_ms = ms.t0 > ms.ta ? (double)(ms.t0 - ms.ta) * 1e-6 : 0.0;
       st.latency_ms = t1 > ms.ta ? (double)(t1 - ms.ta) * 1e-6 : 0.0;
-      stats[mi] = st;
+      io.stats[mi] = st;
     }
   }
   __syncthreads();
@@ -260,7 +348,7 @@ __host__ __device__ inline SmemLayout smem_layout(int n, int nreac, int nchunk) 
   L.part = takec(8 * (size_t)nchunk);
   L.dfa = takec(8 * (size_t)nreac);
   L.dfb = takec(8 * (size_t)nreac);
-  L.vec = takec(8 * 1024);
+  L.vec = takec(8 * (size_t)JAC_VEC_DOUBLES);
   L.aux = L.dfa;
   L.lu = u0;
   size_t lu_end = u0 + lu_smem_bytes<T>(n);
@@ -283,6 +371,8 @@ __device__ Ctx<T> make_ctx(const DevNet* N, Shared* sh, char* smem, const SmemLa
   return C;
 }
 
+// per-slot workspace in global memory, sized for the context's largest
+// network (n = NEQ, nreac reactions)
 template <typename T>
 struct SlotArrays {
   double* yh;
@@ -292,10 +382,13 @@ struct SlotArrays {
   int* perm;
   T* scr;
   T* dinv;
+  double* jpart;
+  int n, nreac, njch;
 };
 
 template <typename T>
-__device__ __forceinline__ Slot<T> slot_of(const SlotArrays<T>& A, int s, int n, int nreac) {
+__device__ __forceinline__ Slot<T> slot_of(const SlotArrays<T>& A, int s) {
+  const int n = A.n, nreac = A.nreac;
   Slot<T> W;
   W.yh = nullptr;  // shared memory, set by make_ctx
   W.rate = A.rate + (size_t)s * nreac;
@@ -304,6 +397,7 @@ __device__ __forceinline__ Slot<T> slot_of(const SlotArrays<T>& A, int s, int n,
   W.perm = A.perm + (size_t)s * n;
   W.scr = A.scr + (size_t)s * 2 * LuCfg<T>::NB * n;
   W.dinv = A.dinv + (size_t)s * dinv_elems(n);
+  W.jpart = A.jpart + (size_t)s * A.njch;
   return W;
 }
 
@@ -356,48 +450,109 @@ __global__ void __launch_bounds__(1024) k_order(const ucl_model_params* params, 
   for (int i = tid; i < nmodels; i += blockDim.x) order[i] = idx[i];
 }
 
+// Live request queue of the serving mode: a ring of `cap` records whose
+// parameters and flags live in host-pinned memory mapped into the device's
+// address space.  Request k (numbered from 0) uses record k % cap: its
+// parameters are req[k % cap], its outputs the record's rows of the solve's
+// output arrays.  The host publishes request k by writing req[k % cap] and
+// then tail = k + 1 (release); it publishes request k only after it has
+// taken the outputs of request k - cap, so a record is never overwritten
+// while in use.  The device sets done[k % cap] = k + 1 (release, after the
+// outputs are written).  closed = 1 ends the session once every published
+// request is claimed.
+struct LiveQueue {
+  const ucl_model_params* req;  // [cap]
+  const unsigned* tail;
+  const unsigned* closed;
+  unsigned* done;               // [cap]
+  int* status;                  // set to UCL_E_TIMEOUT by a CTA whose wait gave up
+  int cap;
+  unsigned idle_limit;          // sleeps of 20 us an idle CTA waits for a request before it gives up
+};
+
+__device__ __forceinline__ unsigned ld_acquire_sys(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.sys.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_sys(unsigned* p, unsigned v) {
+  asm volatile("st.release.sys.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 // Persistent solver: each CTA pulls model indices from a device counter
-// (requests in index order, or through `order` when given).  The launch epoch is the first CTA's start
-// time.  With an arrival schedule (seconds after the epoch, ascending), a
-// request is not started before its arrival; queue and latency times are
-// measured from arrival (from the epoch without a schedule).
+// (requests in index order, or through `order` when given).  The launch
+// epoch is the first CTA's start time.  With an arrival schedule (seconds
+// after the epoch, ascending), a request is not started before its arrival;
+// queue and latency times are measured from arrival (from the epoch without
+// a schedule).  With a live queue (q.cap > 0) the counter numbers requests
+// that the host appends while the kernel runs (LiveQueue).  A model's
+// network tables are loaded into shared memory when it differs from the
+// previous model's network.
 template <typename T>
-__global__ void __launch_bounds__(NT, 1) k_solve_models(DevNet N, const ucl_model_params* params, const double* start,
-                                                     int nmodels, int max_rows, double* phys_out, double* abund_out,
-                                                     int* nrows_out, int* flag_out, ucl_model_stats* stats,
-                                                     SlotArrays<T> ws, int* counter, unsigned long long* epoch,
-                                                     const double* arrival_s, const int* order) {
+__global__ void __launch_bounds__(NT, 1) k_solve_models(SolveIO io, SlotArrays<T> ws, int* counter,
+                                                     unsigned long long* epoch, const double* arrival_s,
+                                                     const int* order, LiveQueue q) {
   extern __shared__ __align__(16) char smem[];
   __shared__ Shared sh;
   __shared__ DevNet sN;
-  if (threadIdx.x == 0) sN = N;
-  const SmemLayout L = smem_layout<T>(N.neq, N.nreac, N.npart);
-  __syncthreads();
-  Ctx<T> C = make_ctx<T>(&sN, &sh, smem, L, slot_of(ws, blockIdx.x, N.neq, N.nreac));
-  if constexpr (sizeof(T) == 4) tc_setup(&sh.tc);
   __shared__ unsigned long long t_epoch;
+  __shared__ unsigned req_no;
+  const int nmodels = io.nmodels;
+  if constexpr (sizeof(T) == 4) tc_setup(&sh.tc);
   if (threadIdx.x == 0) {
     const unsigned long long now = globaltimer_ns();
     const unsigned long long old = atomicCAS(epoch, 0ull, now);
     t_epoch = old ? old : now;
   }
+  int cur_net = -1;
+  Ctx<T> C;
   for (;;) {
     if (threadIdx.x == 0) {
       const int k = atomicAdd(counter, 1);
-      sh.ms.model = (order && k < nmodels) ? order[k] : k;
-      const int mi = sh.ms.model;
       sh.ms.ta = t_epoch;
-      if (mi < nmodels && arrival_s) {
-        const double a = arrival_s[mi];
-        const unsigned long long ta = t_epoch + (a > 0.0 ? (unsigned long long)(a * 1e9) : 0ull);
-        sh.ms.ta = ta;
-        for (unsigned it = 0; it < ADMIT_SLEEP_LIMIT && globaltimer_ns() < ta; ++it) __nanosleep(20000);
+      if (q.cap > 0) {
+        // wait (bounded) until request k is published or the session ends
+        int mi = nmodels;
+        unsigned it = 0;
+        for (; it < q.idle_limit; ++it) {
+          if ((unsigned)k < ld_acquire_sys(q.tail)) { mi = k % q.cap; break; }
+          if (ld_acquire_sys(q.closed)) break;
+          __nanosleep(20000);
+        }
+        if (it == q.idle_limit) atomicExch(q.status, UCL_E_TIMEOUT);
+        sh.ms.ta = globaltimer_ns();
+        req_no = (unsigned)k;
+        sh.ms.model = mi;
+      } else {
+        sh.ms.model = (order && k < nmodels) ? order[k] : k;
+        const int mi = sh.ms.model;
+        if (mi < nmodels && arrival_s) {
+          const double a = arrival_s[mi];
+          const unsigned long long ta = t_epoch + (a > 0.0 ? (unsigned long long)(a * 1e9) : 0ull);
+          sh.ms.ta = ta;
+          for (unsigned it = 0; it < ADMIT_SLEEP_LIMIT && globaltimer_ns() < ta; ++it) __nanosleep(20000);
+        }
       }
     }
     __syncthreads();
     const int mi = sh.ms.model;
     if (mi >= nmodels) break;
-    run_model<T>(C, params, start, mi, max_rows, phys_out, abund_out, nrows_out, flag_out, stats);
+    const int kn = io.net_of ? io.net_of[mi] : 0;
+    if (kn != cur_net) {
+      // this model's network tables into shared memory
+      for (int i = threadIdx.x; i < (int)(sizeof(DevNet) / sizeof(int)); i += NT)
+        reinterpret_cast<int*>(&sN)[i] = reinterpret_cast<const int*>(io.nets + kn)[i];
+      __syncthreads();
+      cur_net = kn;
+      C = make_ctx<T>(&sN, &sh, smem, smem_layout<T>(sN.neq, sN.nreac, sN.nchunk), slot_of(ws, blockIdx.x));
+    }
+    SolveIO mio = io;
+    if (q.cap > 0) mio.params = q.req;
+    run_model<T>(C, mio, mi);
+    if (q.cap > 0 && threadIdx.x == 0) {
+      __threadfence_system();
+      st_release_sys(q.done + mi, req_no + 1u);
+    }
   }
   if constexpr (sizeof(T) == 4) tc_teardown(&sh.tc);
 }
@@ -413,7 +568,7 @@ __global__ void __launch_bounds__(NT) k_lu_batch(T* mats, int n, int* perm, int*
   const int s = blockIdx.x;
   if (s >= nsys) return;
   const bool use_tc = LuSmem<T>::tc_ok(n);
-  if (use_tc) tc_setup(&tc);
+  if (use_tc) tc_setup(&tc, tc_cols_for(n));
   const int r = block_lu<T>(mats + (size_t)s * n * n, n, perm + (size_t)s * n, smem, si,
                             scr + (size_t)s * 2 * LuCfg<T>::NB * n, lperm, use_tc ? &tc : nullptr);
   if (threadIdx.x == 0) info[s] = r;
@@ -429,7 +584,7 @@ __global__ void __launch_bounds__(NT) k_lu_batch_strided(T* mats, int n, int* pe
   __shared__ int lperm[MAX_NEQ];
   __shared__ TcState tc;
   const bool use_tc = LuSmem<T>::tc_ok(n);
-  if (use_tc) tc_setup(&tc);
+  if (use_tc) tc_setup(&tc, tc_cols_for(n));
   T* my_scr = scr + (size_t)blockIdx.x * 2 * LuCfg<T>::NB * n;
   for (int s = blockIdx.x; s < nsys; s += gridDim.x) {
     const int r = block_lu<T>(mats + (size_t)s * n * n, n, perm + (size_t)s * n, smem, si, my_scr, lperm,
@@ -458,6 +613,7 @@ __global__ void __launch_bounds__(NT) k_rates(DevNet N, const ucl_model_params* 
     S.Td = S.T;
     S.av = av[s];
     S.phi = phi[s];
+    S.h2crp = 0.0;  // the first interval's h2CRPRate
     S.cs = (sh.P.rout - sh.P.rin) * cK.PC / (double)(float)sh.P.points;
   }
   __syncthreads();
@@ -470,10 +626,15 @@ __global__ void __launch_bounds__(NT) k_rates(DevNet N, const ucl_model_params* 
     double sb = 0.0, ss = 0.0;
     for (int i = 0; i < N.n_bulk; i++) sb = i == 0 ? y[N.bulk_list[i]] : sb + y[N.bulk_list[i]];
     for (int i = 0; i < N.n_surface; i++) ss = i == 0 ? y[N.surface_list[i]] : ss + y[N.surface_list[i]];
-    y[N.nbulk] = sb;
-    y[N.nsurf] = ss;
+    if (N.n_bulk > 0) y[N.nbulk] = sb;
+    if (N.n_surface > 0) y[N.nsurf] = ss;
     S.sm = fmax(1e-30, ss);
     S.sb = fmax(1e-30, sb);
+    if (N.n_refr > 0) {
+      double r = 0.0;
+      for (int i = 0; i < N.n_refr; i++) r += y[N.refr_list[i]];
+      S.sb = S.sb - r;
+    }
     const double q = cK.NUM_SITES_PER_GRAIN / (cK.GAS_DUST_DENSITY_RATIO * S.sb);
     S.blr = q < 1.0 ? q : 1.0;
     photo_setup(S, sh.P.radfield);
@@ -487,7 +648,7 @@ __global__ void __launch_bounds__(NT) k_rates(DevNet N, const ucl_model_params* 
 // RHS (ucl_rhs_batch) or RHS + analytic Jacobian (ucl_jac_batch), one CTA per system.
 __global__ void __launch_bounds__(NT) k_rhs_jac(DevNet N, const ucl_model_params* params, const double* yin,
                                                 const double* rates, const double* av, double* ydot, double* jac,
-                                                int nsys) {
+                                                double* jpart, int nsys) {
   extern __shared__ __align__(16) char smem[];
   __shared__ Shared sh;
   const int s = blockIdx.x;
@@ -497,7 +658,7 @@ __global__ void __launch_bounds__(NT) k_rhs_jac(DevNet N, const ucl_model_params
   double* out = y + n;
   double* flux = out + n;
   double* part = flux + N.nreac;
-  double* dfa = part + N.npart;
+  double* dfa = part + N.nchunk;
   double* dfb = dfa + N.nreac;
   double* vec = dfb + N.nreac;
   for (int i = threadIdx.x; i < n; i += NT) y[i] = yin[(size_t)s * n + i];
@@ -514,7 +675,7 @@ __global__ void __launch_bounds__(NT) k_rhs_jac(DevNet N, const ucl_model_params
     for (int i = threadIdx.x; i < n; i += NT) ydot[(size_t)s * n + i] = out[i];
   if (jac)
     dev_jac<false, double>(N, sh.P, sh.S, y, r, nullptr, nullptr, jac + (size_t)s * n * n, flux, dfa, dfb, vec,
-                           part, sh.R);
+                           jpart + (size_t)s * N.njch, sh.R);
 }
 
 }  // namespace ucl

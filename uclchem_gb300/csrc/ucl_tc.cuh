@@ -22,7 +22,7 @@
 
 namespace ucl {
 
-constexpr int TC_TMEM_COLS = 512;       // accumulator columns allocated per CTA
+constexpr int TC_TMEM_COLS = 512;       // most accumulator columns a CTA allocates
 constexpr int TC_M = 128;               // rows per tcgen05.mma
 constexpr unsigned TC_WAIT_LIMIT = 1u << 22;  // bounded mbarrier polling
 
@@ -32,22 +32,32 @@ struct TcState {
   unsigned tmem;            // TMEM base address from tcgen05.alloc
   unsigned phase;           // parity of the next mbarrier phase to wait for
   int err;                  // set when a bounded wait gave up
+  unsigned cols;            // TMEM columns held (a power of two, 32..512)
 };
+
+// TMEM columns the trailing updates of an n x n FP32 factorisation need:
+// the widest update is the first one, n - 32 columns padded to 16, and the
+// allocation is a power of two of at least 32.  Sizing it to n lets more
+// than one CTA hold TMEM on an SM where shared memory allows it.
+__host__ __device__ constexpr unsigned tc_cols_for(int n) {
+  return ((n - 32 + 15) & ~15) <= 32 ? 32u : ((n - 32 + 15) & ~15) <= 64 ? 64u
+       : ((n - 32 + 15) & ~15) <= 128 ? 128u : ((n - 32 + 15) & ~15) <= 256 ? 256u : 512u;
+}
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) {
   return (unsigned)__cvta_generic_to_shared(p);
 }
 
-// warp-collective: allocate TC_TMEM_COLS columns, address to *dst
-__device__ __forceinline__ void tc_alloc(unsigned* dst) {
+// warp-collective: allocate `cols` columns, address to *dst
+__device__ __forceinline__ void tc_alloc(unsigned* dst, unsigned cols) {
   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(dst)),
-               "r"((unsigned)TC_TMEM_COLS)
+               "r"(cols)
                : "memory");
   asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
 }
 // warp-collective
-__device__ __forceinline__ void tc_dealloc(unsigned taddr) {
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"((unsigned)TC_TMEM_COLS)
+__device__ __forceinline__ void tc_dealloc(unsigned taddr, unsigned cols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(cols)
                : "memory");
 }
 __device__ __forceinline__ void tc_fence_before() {
@@ -121,9 +131,10 @@ __device__ __forceinline__ void tc_ld_wait() { asm volatile("tcgen05.wait::ld.sy
 
 // CTA prologue / epilogue of kernels that use the tensor cores: TMEM
 // allocation by warp 0, mbarrier set-up by thread 0.  All threads call.
-__device__ __forceinline__ void tc_setup(TcState* tc) {
-  if ((threadIdx.x >> 5) == 0) tc_alloc(&tc->tmem);
+__device__ __forceinline__ void tc_setup(TcState* tc, unsigned cols = TC_TMEM_COLS) {
+  if ((threadIdx.x >> 5) == 0) tc_alloc(&tc->tmem, cols);
   if (threadIdx.x == 0) {
+    tc->cols = cols;
     mbar_init(&tc->mbar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     tc->phase = 0;
@@ -137,7 +148,7 @@ __device__ __forceinline__ void tc_teardown(TcState* tc) {
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if ((threadIdx.x >> 5) == 0) tc_dealloc(tc->tmem);
+  if ((threadIdx.x >> 5) == 0) tc_dealloc(tc->tmem, tc->cols);
 }
 
 // TF32 head (round to nearest, ties away) of x, as an FP32 value

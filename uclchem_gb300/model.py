@@ -62,26 +62,30 @@ def _start_vectors(ctx: Context, params, starting_chemistry, n: int):
 
 
 def cloud_grid(param_dicts: Sequence[Optional[dict]], timepoints: int = TIMEPOINTS,
-               starting_chemistry=None, precision="mixed", context: Optional[Context] = None):
+               starting_chemistry=None, precision="mixed", context: Optional[Context] = None,
+               return_rates: bool = False):
     """Run many static/freefall CLOUD models in one device launch.
 
     Returns (physics [n, rows, 8], abundances [n, rows, nspec], nrows [n],
-    flags [n], stats [n]) with rows = timepoints + 1.
+    flags [n], stats [n]) with rows = timepoints + 1, and the rates rows
+    [n, rows, nreac] (the reference's ratesarray) when return_rates is set.
     """
     ctx = context or get_context()
     params = make_param_array(param_dicts)
     start = _start_vectors(ctx, params, starting_chemistry, len(params))
-    return ctx.solve_models(params, timepoints + 1, start=start, precision=_precision(precision))
+    return ctx.solve_models(params, timepoints + 1, start=start, precision=_precision(precision),
+                            rates=return_rates)
 
 
 def cloud(param_dict=None, out_species: Optional[List[str]] = None, return_array: bool = False,
           return_dataframe: bool = False, return_rates: bool = False, starting_chemistry=None,
           timepoints: int = TIMEPOINTS, precision="mixed"):
-    """Single CLOUD model with the reference's calling convention."""
-    if return_rates:
-        raise UclError("return_rates is not available on the device path")
+    """Single CLOUD model with the reference's calling convention
+    (pre_flight_checklist's argument rules, model.py:102-160)."""
     if starting_chemistry is not None and not (return_array or return_dataframe):
         raise AssertionError("starting_chemistry can only be used with return_array or return_dataframe set to True")
+    if return_rates and not (return_array or return_dataframe):
+        raise AssertionError("return_rates can only be used with return_array or return_dataframe set to True")
     pd = dict(param_dict or {})
     file_keys = [k for k in pd if k.lower().endswith("file")]
     if file_keys:
@@ -94,21 +98,24 @@ def cloud(param_dict=None, out_species: Optional[List[str]] = None, return_array
         if return_array or return_dataframe:
             return None, None, None, None, flag
         return [flag]
-    phys, ab, nrows, flags, _ = cloud_grid([pd], timepoints=timepoints, starting_chemistry=starting_chemistry,
-                                           precision=precision, context=ctx)
+    out = cloud_grid([pd], timepoints=timepoints, starting_chemistry=starting_chemistry,
+                     precision=precision, context=ctx, return_rates=return_rates)
+    phys, ab, nrows, flags = out[:4]
     n = int(nrows[0])
     flag = int(flags[0])
     species = _network.load_default().species
     phys_a = phys[0, :n, None, :]
     chem_a = ab[0, :n, None, :]
+    rates_a = out[5][0, :n, None, :] if return_rates else None
     abundance_start = ab[0, n - 1, :] if n > 0 else None
     if return_dataframe:
         import pandas as pd_  # not a dependency of the device path
         physics_df = pd_.DataFrame(phys_a[:, 0, :], columns=PHYSICAL_PARAMETERS)
         chem_df = pd_.DataFrame(chem_a[:, 0, :], columns=species)
-        return physics_df, chem_df, None, abundance_start, flag
+        rates_df = pd_.DataFrame(rates_a[:, 0, :]) if return_rates else None
+        return physics_df, chem_df, rates_df, abundance_start, flag
     if return_array:
-        return phys_a, chem_a, None, abundance_start, flag
+        return phys_a, chem_a, rates_a, abundance_start, flag
     if flag < 0 or not out_species:
         return [flag]
     idx = [species.index(s) for s in out_species]

@@ -393,6 +393,8 @@ class Network:
         add("stoich_ptr", self.stoich_ptr, 1)
         add("stoich_rx", self.stoich_rx, 1)
         add("stoich_coef", self.stoich_coef, 1)
+        # positive ions for enforceChargeConservation (chemistry.f90:114-121)
+        add("ion_list", [i for i, name in enumerate(self.species) if "+" in name], 1)
         return _BLOB_MAGIC + b"".join(recs)
 
 

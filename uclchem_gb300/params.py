@@ -39,6 +39,7 @@ class ModelParams(ctypes.Structure):
         "desorb", "h2desorb", "crdesorb", "uvdesorb", "thermdesorb",
         "ion", "points", "mxstep",
         "enforceChargeConservation", "improvedH2CRPDissociation",
+        "cosmicRayAttenuation", "ionModel",
     )]
 
 
@@ -63,6 +64,7 @@ DEFAULTS: Dict[str, float] = {
     "freefall": 0, "endAtFinalDensity": 0, "desorb": 1, "h2desorb": 1, "crdesorb": 1,
     "uvdesorb": 1, "thermdesorb": 1, "ion": 2, "points": 1, "mxstep": 10000,
     "enforceChargeConservation": 0, "improvedH2CRPDissociation": 0,
+    "cosmicRayAttenuation": 0, "ionModel": ord("L"),
 }
 
 # dictionaryParser keys (lower case) -> struct field (wrap.f90:755-975)
@@ -71,7 +73,7 @@ _KEYMAP["thermdesorb"] = "uvdesorb"        # quirk Q2 (wrap.f90:802-803)
 # accepted keys that do not reach the chemistry path
 _IGNORED = {"outspecies", "writestep", "abundsavefile", "abundloadfile", "outputfile",
             "ratefile", "fluxfile", "columnfile", "ntime", "bm0", "instantsublimation",
-            "cosmicrayattenuation", "ionmodel", "currenttime"}
+            "currenttime"}
 _NOT_PARSED = {"mxstep", "enforcechargeconservation"}  # module variables without a dict key
 
 
@@ -88,6 +90,15 @@ def _to_bool(v) -> int:
             return 0
         raise ParameterError(f"not a logical: {v!r}")
     return int(bool(v))
+
+
+def _to_char(v) -> int:
+    """A Fortran CHARACTER(1) read of the value: its first character (list-
+    directed READ strips the surrounding quotes), as a character code."""
+    s = str(v).strip().strip("'\"")
+    if not s:
+        raise ParameterError(f"not a character: {v!r}")
+    return ord(s[0])
 
 
 def make_params(param_dict: Optional[dict] = None) -> np.ndarray:
@@ -113,7 +124,9 @@ def make_params(param_dict: Optional[dict] = None) -> np.ndarray:
             field = _KEYMAP[lk]
             kind = PARAMS_DTYPE[field]
             try:
-                if kind == np.int32:
+                if field == "ionModel":
+                    rec[field] = _to_char(v)
+                elif kind == np.int32:
                     rec[field] = _to_bool(v) if field not in ("ion", "points") else int(v)
                 else:
                     rec[field] = float(v)

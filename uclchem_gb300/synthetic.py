@@ -184,3 +184,64 @@ def jacobian(net: SyntheticNetwork, y: np.ndarray) -> np.ndarray:
             if b >= 0:
                 J[s, b] += sign * db
     return J
+
+
+def to_network(net: SyntheticNetwork):
+    """The synthetic network as a compiled :class:`uclchem_gb300.network.Network`
+    (the table compiler's input form), so it loads through the same C ABI as
+    a MakeRates network.  Every reaction sits in the two-body range with
+    beta = gamma = 0, so its device rate is exactly alpha (the constant k);
+    two-body fluxes have the RATE*D*Y*Y shape and one-body fluxes RATE*Y.
+    There are no ices, no self-shielded photo reactions and no named species:
+    the named-species slots point at the density slot, as UCLCHEM does for
+    elements a network lacks, and the named reactions are absent (-1)."""
+    from .network import (REACTION_PARAMS, SPECIES_PARAMS, RANGE_NAMES, Network)
+    n, m = net.nspec, net.nreac
+    empty_i = np.zeros(0, dtype=np.int32)
+    empty_d = np.zeros(0, dtype=np.float64)
+    ranges = {k: (99999, 99999) for k in RANGE_NAMES}
+    ranges["twobodyReacs"] = (1, m)
+    re = -np.ones((m, 3), dtype=np.int32)
+    re[:, :2] = net.reactants
+    pr = -np.ones((m, 4), dtype=np.int32)
+    pr[:, :2] = net.products
+    two = net.reactants[:, 1] >= 0
+    shape = np.where(two, 0, 1).astype(np.int32)
+    terms = []
+    for r, ((a, b), (c, d)) in enumerate(zip(net.reactants, net.products)):
+        for s, sign in ((a, -1), (b, -1), (c, 1), (d, 1)):
+            if s >= 0:
+                terms.append((s, sign, r, int(shape[r]), int(a), int(b)))
+    out = Network(
+        nspec=n, nreac=m, species=list(net.names),
+        mass=np.ones(n), atom_counts=np.zeros(n, dtype=np.int32),
+        surface_list=empty_i, bulk_list=empty_i, ice_list=empty_i, gas_ice_list=empty_i,
+        refractory_list=empty_i, binding_energy=empty_d, formation_enthalpy=empty_d,
+        three_phase=False, sp={k: n for k in SPECIES_PARAMS}, rx={k: -1 for k in REACTION_PARAMS},
+        re=re, pr=pr, alpha=np.asarray(net.k, dtype=np.float64), beta=np.zeros(m), gama=np.zeros(m),
+        min_temps=np.zeros(m), max_temps=np.full(m, 1e10), reduced_masses=np.zeros(m),
+        extrapolate=np.ones(m, dtype=bool), freeze_partners=empty_i, gar_params=np.zeros((0, 7)),
+        ranges=ranges, terms=np.array(terms, dtype=np.int32).reshape(-1, 6),
+        swap_terms=np.zeros((0, 2), dtype=np.int32), tr_surface=empty_i, tr_bulk=empty_i,
+    )
+    out.flux_shape = shape
+    out.flux_ya = np.ascontiguousarray(net.reactants[:, 0], dtype=np.int32)
+    out.flux_yb = np.ascontiguousarray(net.reactants[:, 1], dtype=np.int32)
+    out.stoich_ptr = np.ascontiguousarray(net.stoich_ptr, dtype=np.int32)
+    out.stoich_rx = np.ascontiguousarray(net.stoich_rx, dtype=np.int32)
+    out.stoich_coef = np.ascontiguousarray(net.stoich_coef, dtype=np.int32)
+    return out
+
+
+def write_blob(net: SyntheticNetwork, path: str) -> str:
+    """Write the network's UCLNET01 blob (ucl_network_load's input)."""
+    with open(path, "wb") as f:
+        f.write(to_network(net).to_blob())
+    return path
+
+
+def start_vectors(net: SyntheticNetwork, nsys: int, seed: int = 20261203) -> np.ndarray:
+    """[nsys, N+1] start vectors of the device solver: the seeded initial
+    abundances and the network's density in the last (density) slot."""
+    y = initial_abundances(net, nsys, seed)
+    return np.concatenate([y, np.full((nsys, 1), net.density)], axis=1)
