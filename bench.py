@@ -75,6 +75,9 @@ def parse():
                                                 "timed grid (and of the FP64 sample) to this .npz")
     ap.add_argument("--serve", type=int, default=0, help="serving run: number of Poisson-arriving requests")
     ap.add_argument("--rate", type=float, default=20.0, help="serving arrival rate (requests/s)")
+    ap.add_argument("--serve-capacity", type=int, default=4096, help="request/output records of the server")
+    ap.add_argument("--synthetic", type=int, default=0,
+                    help="synthetic-network run: systems per network size (N = 64, 128, 256, 512), one launch")
     ap.add_argument("--kernel", default="solve", choices=["solve", "lu"],
                     help="lu: time the batched Newton-matrix LU alone (--models matrices)")
     return ap.parse_args()
@@ -502,45 +505,136 @@ def serve_requests(n: int, seed: int = SEED):
 
 
 def serve_arm(args):
-    """Poisson request stream through ucl_serve_models_device: requests are
-    admitted on the device at their arrival times; p50/p99 latency (arrival
-    to completion) and completed models/s."""
-    import torch
+    """A live serving session (ucl_server_*): the persistent solver is
+    launched once; a host thread submits requests at Poisson arrival times
+    while it runs (backpressure when the ring is full counts as latency);
+    the main thread polls completions and takes each result.  Latency is
+    host-observed, from a request's arrival time to the poll that sees it
+    done; throughput is completed requests over the session's wall time."""
     from uclchem_gb300 import _lib, network
     from uclchem_gb300.params import make_param_array
     ctx = _lib.Context(network.DEFAULT_BLOB, device=0)
-    stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
     n, rows = args.serve, 160
-    reqs = serve_requests(n)
-    params = make_param_array(reqs)
+    params = make_param_array(serve_requests(n))
     rng = np.random.default_rng(SEED + 11)
     arrival = np.cumsum(rng.exponential(1.0 / args.rate, n))
+    srv = _lib.Server(ctx, capacity=args.serve_capacity, max_rows=rows, precision=_lib.PREC_MIXED)
+    t_arr = np.zeros(n)
+    t_done = np.full(n, np.nan)
+    flags = np.zeros(n, dtype=np.int32)
+    solve_ms = np.zeros(n)
+    submitted = [0]
+
+    def submitter():
+        for k in range(n):
+            due = t0 + arrival[k]
+            while time.perf_counter() < due:
+                time.sleep(min(0.002, max(0.0, due - time.perf_counter())))
+            t_arr[k] = due
+            while srv.submit(params[k]) is None:  # ring full: wait for takes
+                time.sleep(0.0005)
+            submitted[0] = k + 1
+
+    t0 = time.perf_counter()
+    th = threading.Thread(target=submitter, daemon=True)
+    th.start()
+    done = 0
+    nxt = 0
+    pending = []
+    while done < n:
+        while nxt < submitted[0]:
+            pending.append(nxt)
+            nxt += 1
+        still = []
+        for k in pending:
+            if srv.poll(k):
+                t_done[k] = time.perf_counter()
+                _, _, _, fl, st = srv.take(k)
+                flags[k] = fl
+                solve_ms[k] = st["solve_ms"]
+                done += 1
+            else:
+                still.append(k)
+        pending = still
+        time.sleep(0.001)
+    wall = time.perf_counter() - t0
+    th.join()
+    srv.close()
+    lat = (t_done - t_arr) * 1e3
+    print(json.dumps({"mode": "serving", "requests": n, "arrival_rate_per_s": args.rate,
+                      "mix": "70% static CLOUD, 30% freefall 1e2->1e6; finalTime 10^U(4,7) yr",
+                      "server": f"live request ring of {srv.capacity} records, {rows} rows each, mixed precision",
+                      "models_per_s": n / wall, "wall_s": wall,
+                      "p50_latency_ms": float(np.percentile(lat, 50)), "p99_latency_ms": float(np.percentile(lat, 99)),
+                      "p50_solve_ms": float(np.percentile(solve_ms, 50)),
+                      "p99_solve_ms": float(np.percentile(solve_ms, 99)),
+                      "latency": "host-observed: Poisson arrival time to the poll that sees the request done",
+                      "failed": int((flags != 0).sum()), "slots": ctx.slots(_lib.PREC_MIXED)}), flush=True)
+    ctx.close()
+
+
+def synthetic_arm(args):
+    """Synthetic mass-action networks of four sizes (N = 64, 128, 256, 512,
+    10 N reactions), --synthetic systems each, all in one launch of a
+    multi-network context (mixed precision: FP64 state, FP32 LU), to 1e6 yr:
+    models/s, p50/p99 per-model time, and element/charge conservation."""
+    import tempfile
+    import torch
+    from uclchem_gb300 import _lib
+    from uclchem_gb300 import synthetic as S
+    per = args.synthetic
+    nets = [S.make_network(n) for n in S.SIZES]
+    with tempfile.TemporaryDirectory() as d:
+        paths = [S.write_blob(net, os.path.join(d, f"syn{net.nspec}.uclnet")) for net in nets]
+        ctx = _lib.Context(paths, device=0)
+    net_of = np.repeat(np.arange(len(nets), dtype=np.int32), per)
+    starts = np.zeros((len(net_of), ctx.neq))
+    for k, net in enumerate(nets):
+        starts[k * per:(k + 1) * per, : net.nspec + 1] = S.start_vectors(net, per)
+    from uclchem_gb300.params import make_param_array
+    params = make_param_array([{"initialDens": nets[k].density, "finalTime": 1e6} for k in net_of])
+    M, rows = len(net_of), 64
     dev = torch.device("cuda", 0)
-    p_d = torch.from_numpy(params.view(np.uint8).reshape(n, -1).copy()).to(dev)
-    a_d = torch.from_numpy(arrival).to(dev)
-    ph = torch.empty((n, rows, 8), dtype=torch.float64, device=dev)
-    ab = torch.empty((n, rows, ctx.nspec), dtype=torch.float64, device=dev)
-    nr = torch.empty(n, dtype=torch.int32, device=dev)
-    fl = torch.empty(n, dtype=torch.int32, device=dev)
-    sd = torch.empty((n, _lib.STATS_DTYPE.itemsize), dtype=torch.uint8, device=dev)
+    p_d = torch.from_numpy(params.view(np.uint8).reshape(M, -1).copy()).to(dev)
+    s_d = torch.from_numpy(starts).to(dev)
+    n_d = torch.from_numpy(net_of).to(dev)
+    ph = torch.zeros((M, rows, 8), dtype=torch.float64, device=dev)
+    ab = torch.zeros((M, rows, ctx.nspec), dtype=torch.float64, device=dev)
+    nr = torch.zeros(M, dtype=torch.int32, device=dev)
+    fl = torch.zeros(M, dtype=torch.int32, device=dev)
+    st = torch.zeros((M, _lib.STATS_DTYPE.itemsize), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(device=dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
     e0.record(stream)
-    ctx.serve_models_device(n, p_d.data_ptr(), a_d.data_ptr(), None, rows, ph.data_ptr(), ab.data_ptr(),
-                            nr.data_ptr(), fl.data_ptr(), sd.data_ptr(), _lib.PREC_MIXED, 0, stream.cuda_stream)
+    ctx.solve_models_nets_device(M, n_d.data_ptr(), p_d.data_ptr(), s_d.data_ptr(), rows, ph.data_ptr(),
+                                 ab.data_ptr(), nr.data_ptr(), fl.data_ptr(), st.data_ptr(), _lib.PREC_MIXED, 0,
+                                 stream.cuda_stream)
     e1.record(stream)
     stream.synchronize()
     ms = e0.elapsed_time(e1)
-    st = sd.cpu().numpy().view(_lib.STATS_DTYPE).reshape(n)
-    flags = fl.cpu().numpy()
-    lat = st["latency_ms"]
-    print(json.dumps({"mode": "serving", "requests": n, "arrival_rate_per_s": args.rate,
-                      "mix": "70% static CLOUD, 30% freefall 1e2->1e6; finalTime 10^U(4,7) yr",
-                      "models_per_s": n / (ms / 1e3), "wall_ms": ms,
-                      "p50_latency_ms": float(np.percentile(lat, 50)), "p99_latency_ms": float(np.percentile(lat, 99)),
-                      "p50_queue_ms": float(np.percentile(st["queue_ms"], 50)),
-                      "p99_queue_ms": float(np.percentile(st["queue_ms"], 99)),
-                      "failed": int((flags != 0).sum()), "slots": ctx.slots(_lib.PREC_MIXED)}), flush=True)
+    stats = st.cpu().numpy().view(_lib.STATS_DTYPE).reshape(M)
+    flags, nrows, abund = fl.cpu().numpy(), nr.cpu().numpy(), ab.cpu().numpy()
+    drift = 0.0
+    per_size = {}
+    for k, net in enumerate(nets):
+        E = net.conserved().astype(float)
+        sel = np.nonzero((net_of == k) & (flags == 0))[0]
+        for i in sel:
+            y = abund[i, : nrows[i], : net.nspec]
+            tot = y @ E.T
+            drift = max(drift, float((np.abs(tot - tot[0]) / (np.abs(y[0]) @ np.abs(E).T)).max()))
+        per_size[str(net.nspec)] = {"p50_ms": float(np.percentile(stats["solve_ms"][net_of == k], 50)),
+                                    "failed": int((flags[net_of == k] != 0).sum())}
+    print(json.dumps({"mode": "synthetic", "sizes": list(S.SIZES), "systems_per_size": per, "models": M,
+                      "final_time_yr": 1e6, "models_per_s": M / (ms / 1e3), "ms": ms,
+                      "p50_ms": float(np.percentile(stats["solve_ms"], 50)),
+                      "p99_ms": float(np.percentile(stats["solve_ms"], 99)),
+                      "failed": int((flags != 0).sum()), "per_size": per_size,
+                      "max_conservation_drift": drift,
+                      "conservation": "element (H, C, O, N) and charge totals per row, relative to the sum of "
+                                      "their terms' magnitudes",
+                      "slots": ctx.slots(_lib.PREC_MIXED)}), flush=True)
     ctx.close()
 
 
@@ -548,6 +642,9 @@ def main():
     args = parse()
     if args.serve > 0:
         serve_arm(args)
+        return
+    if args.synthetic > 0:
+        synthetic_arm(args)
         return
     if args.kernel == "lu":
         lu_kernel(args)

@@ -1,0 +1,96 @@
+"""Generate the grid-parity fixture: the oracle (the CPU restatement of the
+reference's rates + GETYDOT + DVODE MF=22 path) on a seeded sample of the
+4096-point static CLOUD grid, to 1e6 yr with the reference's 501 output rows.
+
+* grid_sample_1e6yr.npz  64 grid points stratified over density, at the
+  reference's tolerances (reltol 1e-8, abstol_factor 1e-14): per model the
+  flag, rows, DVODE counters, output times and every row's log10 abundances
+  (int16 milli-dex, clamped at -16 dex: only species above 1e-14 are
+  compared), and the oracle's CPU time; plus, for every 8th model of the
+  sample, the same model at reltol 1e-12 (mxstep 100000) as the "truth" for
+  the mixed-precision error statement.
+
+The runs take the oracle tens of CPU-minutes per slow model; they run in a
+process pool.  Usage: python tests/golden/make_grid_sample.py [--procs N]
+"""
+import argparse
+import multiprocessing as mp
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+SEED = 20261203
+SAMPLE = 64
+ROWS = 501
+FLOOR_MDEX = -16000
+
+
+def quantize(ab):
+    """log10 abundances in milli-dex as int16, clamped at -16 dex."""
+    q = np.round(1000.0 * np.log10(np.maximum(ab, 1e-30)))
+    return np.clip(q, FLOOR_MDEX, 32000).astype(np.int16)
+
+
+_ORC = None
+
+
+def run(task):
+    global _ORC
+    i, d, tight = task
+    if _ORC is None:
+        from oracle.oracle import Oracle
+        _ORC = Oracle()
+    from uclchem_gb300.params import make_params
+    p = make_params(d)
+    if tight:
+        p["reltol"] = 1e-12
+        p["mxstep"] = 100000
+    t = time.process_time()
+    phys, ab, flag, cnt = _ORC.cloud(p, max_rows=ROWS)
+    return i, tight, int(flag), len(phys), cnt, phys[:, 0].copy(), quantize(ab), time.process_time() - t
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--procs", type=int, default=os.cpu_count() or 1)
+    args = ap.parse_args()
+    from uclchem_gb300.params import grid_params, stratified_sample
+    dicts = grid_params(4096, seed=SEED, final_time=1e6)
+    idx = stratified_sample(dicts, SAMPLE, seed=SEED + 3)
+    tight = idx[::8]
+    tasks = [(i, dicts[i], False) for i in idx] + [(i, dicts[i], True) for i in tight]
+    # longest-expected (densest) first
+    tasks.sort(key=lambda t: -t[1]["initialDens"] * (4 if t[2] else 1))
+    with mp.get_context("spawn").Pool(args.procs) as pool:
+        res = pool.map(run, tasks, chunksize=1)
+    out = {}
+    for tag, sel in (("", False), ("tight_", True)):
+        rr = sorted([r for r in res if r[1] == sel], key=lambda r: (idx if not sel else tight).index(r[0]))
+        m = len(rr)
+        q = np.full((m, ROWS, 335), FLOOR_MDEX, dtype=np.int16)
+        tyr = np.zeros((m, ROWS))
+        for k, r in enumerate(rr):
+            q[k, : r[3]] = r[6]
+            tyr[k, : r[3]] = r[5]
+        out[tag + "index"] = np.array([r[0] for r in rr], dtype=np.int32)
+        out[tag + "flag"] = np.array([r[2] for r in rr], dtype=np.int32)
+        out[tag + "nrows"] = np.array([r[3] for r in rr], dtype=np.int32)
+        out[tag + "counters"] = np.array([r[4] for r in rr], dtype=np.int64)
+        out[tag + "tyears"] = tyr
+        out[tag + "log10_mdex"] = q
+        out[tag + "cpu_s"] = np.array([r[7] for r in rr])
+    np.savez_compressed(os.path.join(HERE, "grid_sample_1e6yr.npz"), seed=SEED, **out)
+    print("wrote", os.path.join(HERE, "grid_sample_1e6yr.npz"))
+    for k in range(len(out["index"])):
+        print(out["index"][k], "%.3g" % dicts[out["index"][k]]["initialDens"], out["flag"][k], out["nrows"][k],
+              out["counters"][k][:4], "%.1f s" % out["cpu_s"][k])
+
+
+if __name__ == "__main__":
+    main()

@@ -150,7 +150,7 @@ __device__ void write_row(Ctx<T>& C, const SolveIO& io, int mi) {
 }
 
 template <typename T>
-__device__ void run_model(Ctx<T>& C, const SolveIO& io, int mi) {
+__device__ void run_model(Ctx<T>& C, const SolveIO& io, int mi, const ucl_model_params* params) {
   const int max_rows = io.max_rows;
   Shared& sh = *C.sh;
   ModelState& ms = sh.ms;
@@ -159,7 +159,7 @@ __device__ void run_model(Ctx<T>& C, const SolveIO& io, int mi) {
   const int tid = threadIdx.x, n = C.n;
   double* y = C.y;
   if (tid == 0) {
-    sh.P = io.params[mi];
+    sh.P = params[mi];
     const ucl_model_params& P = sh.P;
     ms.t0 = globaltimer_ns();
     const double cloudSize = (P.rout - P.rin) * cK.PC;
@@ -505,7 +505,6 @@ __global__ void __launch_bounds__(NT, 1) k_solve_models(SolveIO io, SlotArrays<T
     t_epoch = old ? old : now;
   }
   int cur_net = -1;
-  Ctx<T> C;
   for (;;) {
     if (threadIdx.x == 0) {
       const int k = atomicAdd(counter, 1);
@@ -544,11 +543,9 @@ __global__ void __launch_bounds__(NT, 1) k_solve_models(SolveIO io, SlotArrays<T
         reinterpret_cast<int*>(&sN)[i] = reinterpret_cast<const int*>(io.nets + kn)[i];
       __syncthreads();
       cur_net = kn;
-      C = make_ctx<T>(&sN, &sh, smem, smem_layout<T>(sN.neq, sN.nreac, sN.nchunk), slot_of(ws, blockIdx.x));
     }
-    SolveIO mio = io;
-    if (q.cap > 0) mio.params = q.req;
-    run_model<T>(C, mio, mi);
+    Ctx<T> C = make_ctx<T>(&sN, &sh, smem, smem_layout<T>(sN.neq, sN.nreac, sN.nchunk), slot_of(ws, blockIdx.x));
+    run_model<T>(C, io, mi, q.cap > 0 ? q.req : io.params);
     if (q.cap > 0 && threadIdx.x == 0) {
       __threadfence_system();
       st_release_sys(q.done + mi, req_no + 1u);
