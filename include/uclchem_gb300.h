@@ -293,6 +293,15 @@ int ucl_lu_factor_device(ucl_ctx* ctx, int nsys, int n, int precision, void* mat
 int ucl_lu_factor_device_static(int nsys, int n, int precision, void* mats_dev, int* perm_dev,
                                 int* info_dev, void* stream);
 
+/* The FP32 Newton-matrix LU's trailing update the context's autotuner chose
+ * for network `net`: 1 tensor cores, 0 CUDA cores (or < 0 on error).  At
+ * context creation the autotuner times both on a wave of Newton-like test
+ * matrices of the network's size and keeps the faster; the timings (us per
+ * factorisation, 0 when not measured) are returned through the pointers
+ * (either may be NULL).  UCL_AUTOTUNE=0 in the environment skips the timing
+ * and keeps the tensor cores.  No counterpart in the reference. */
+int ucl_ctx_lu_variant(const ucl_ctx* ctx, int net, float* us_tensor, float* us_cuda);
+
 /* Models the context integrates concurrently at the given precision. */
 int ucl_ctx_slots(const ucl_ctx* ctx, int precision);
 

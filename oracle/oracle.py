@@ -46,6 +46,7 @@ class Oracle:
         lib.orc_get_odes.argtypes = [_vp, _vp, _dp, _dp]
         lib.orc_fd_jacobian.argtypes = [_vp, _vp, _dp, _dp, _dp, ctypes.c_double, _dp]
         lib.orc_photo_rates.argtypes = [_vp, _vp, _dp, _dp]
+        lib.orc_set_cpu_limit.argtypes = [ctypes.c_double]
         self.lib = lib
         path = blob_path or _network.DEFAULT_BLOB
         self.net = lib.orc_net_load(path.encode())
@@ -66,6 +67,13 @@ class Oracle:
             pass
 
     # ------------------------------------------------------------------ #
+    CPU_LIMIT_FLAG = -99
+
+    def set_cpu_limit(self, seconds: float) -> None:
+        """Cap the CPU time of each later model of the calling thread: a
+        model over the cap stops with flag CPU_LIMIT_FLAG (0 = no cap)."""
+        self.lib.orc_set_cpu_limit(float(seconds))
+
     def cloud(self, param_dict=None, start=None, max_rows: int = 501, rates: bool = False):
         """One CLOUD model; returns (phys[rows,8], abund[rows,nspec], flag,
         counters), and the rates rows [rows, nreac] when `rates` is set."""

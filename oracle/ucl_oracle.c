@@ -34,6 +34,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #include "uclchem_gb300.h"
 
@@ -1422,6 +1423,18 @@ L30:
 typedef struct { int64_t nst, nfe, nje, nlu, nni, ncfn, netf; } dv_counts;
 
 /* DVODE driver for ITASK=1, ISTATE=1 (dvode.f90:5654-6766).  Returns ISTATE. */
+/* Optional CPU-time cap of the calling thread's models (a bounded CPU
+ * baseline): a model whose integration has used more than the cap stops
+ * with ORC_CPU_LIMIT.  0 = no cap.                                        */
+#define ORC_CPU_LIMIT (-99)
+static __thread double g_cpu_limit = 0.0, g_cpu_start = 0.0;
+static double thread_cpu_s(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_THREAD_CPUTIME_ID, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+void orc_set_cpu_limit(double seconds) { g_cpu_limit = seconds > 0.0 ? seconds : 0.0; }
+
 static int dvode(dv_t* d, double* y, double* t, double tout, dv_counts* cnt) {
   int n = d->n;
   double* yh = d->yh;
@@ -1485,6 +1498,10 @@ static int dvode(dv_t* d, double* y, double* t, double tout, dv_counts* cnt) {
     }
   }
     dvstep(d, y);
+    if (g_cpu_limit > 0.0 && (d->nst & 63) == 0 && thread_cpu_s() - g_cpu_start > g_cpu_limit) {
+      istate = ORC_CPU_LIMIT;
+      goto L410;
+    }
     if (d->kflag == -1) { istate = -4; goto L410; }
     if (d->kflag == -2) { istate = -5; goto L410; }
     if ((d->tn - tout) * d->h < 0.0) continue;
@@ -1655,6 +1672,8 @@ static int integrate_interval(model_t* m, chem_t* c) {
       break;
     case -3:
       return UCL_INT_UNRECOVERABLE_ERROR;
+    case ORC_CPU_LIMIT:
+      return ORC_CPU_LIMIT;
     default:
       break;
   }
@@ -1723,6 +1742,7 @@ static void write_row(const chem_t* c, const model_t* m, double* phys, double* a
 int orc_cloud_rates(const orc_net* n, const ucl_model_params* p, const double* start, int max_rows, double* phys,
                     double* abund_rows, int* nrows, int64_t* counters /* [9] or NULL */, double* rates_rows) {
   pthread_once(&g_tab_once, init_tables);
+  g_cpu_start = thread_cpu_s();
   chem_t c;
   model_t m;
   memset(&m, 0, sizeof(m));

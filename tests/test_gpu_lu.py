@@ -34,3 +34,19 @@ def test_batched_lu_reconstructs(precision):
         # pivots chosen as in partial pivoting: |L| <= 1
         assert np.abs(np.tril(LU[s], -1)).max() <= 1.0 + 1e-6
     ctx.close()
+
+
+def test_autotuner_picks_the_faster_lu_update(monkeypatch):
+    """The context's autotuner times the FP32 LU's tensor-core and CUDA-core
+    trailing updates for the network's size and keeps the faster;
+    UCL_AUTOTUNE=0 skips the timing and keeps the tensor cores."""
+    from uclchem_gb300 import _lib, network
+    ctx = _lib.Context(network.DEFAULT_BLOB, device=0)
+    tc, us_tc, us_cc = ctx.lu_variant(0)
+    assert us_tc > 0 and us_cc > 0
+    assert tc == (us_tc <= us_cc)
+    ctx.close()
+    monkeypatch.setenv("UCL_AUTOTUNE", "0")
+    ctx = _lib.Context(network.DEFAULT_BLOB, device=0)
+    assert ctx.lu_variant(0) == (True, 0.0, 0.0)
+    ctx.close()

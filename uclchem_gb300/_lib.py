@@ -44,7 +44,8 @@ EXPORTS = ["ucl_params_default", "ucl_network_load", "ucl_network_free", "ucl_ne
            "ucl_ctx_nreac", "ucl_rates_batch", "ucl_rhs_batch", "ucl_jac_batch", "ucl_solve_models",
            "ucl_solve_models_device", "ucl_solve_models_nets_device", "ucl_ctx_slots", "ucl_lu_factor_device",
            "ucl_serve_models_device", "ucl_server_open", "ucl_server_capacity", "ucl_server_submit",
-           "ucl_server_poll", "ucl_server_take", "ucl_server_close", "ucl_lu_factor_device_static"]
+           "ucl_server_poll", "ucl_server_take", "ucl_server_close", "ucl_lu_factor_device_static",
+           "ucl_ctx_lu_variant"]
 
 E_AGAIN = -107
 
@@ -79,6 +80,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         lib.ucl_ctx_destroy.argtypes = [_vp]
         lib.ucl_ctx_nspec.argtypes = [_vp]
         lib.ucl_ctx_nreac.argtypes = [_vp]
+        lib.ucl_ctx_lu_variant.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
+                                           ctypes.POINTER(ctypes.c_float)]
         lib.ucl_rates_batch.argtypes = [_vp, ctypes.c_int, _vp, _dp, _dp, _dp, _dp]
         lib.ucl_rhs_batch.argtypes = [_vp, ctypes.c_int, _vp, _dp, _dp, _dp, _dp]
         lib.ucl_jac_batch.argtypes = [_vp, ctypes.c_int, _vp, _dp, _dp, _dp, _dp]
@@ -160,6 +163,15 @@ class Context:
 
     def slots(self, precision: int) -> int:
         return self.lib.ucl_ctx_slots(self.ctx, precision)
+
+    def lu_variant(self, net: int = 0):
+        """(tensor_cores, us_tensor, us_cuda): the autotuner's FP32 LU choice
+        for network `net` and its timings."""
+        a, b = ctypes.c_float(0), ctypes.c_float(0)
+        v = self.lib.ucl_ctx_lu_variant(self.ctx, net, ctypes.byref(a), ctypes.byref(b))
+        if v < 0:
+            raise UclError(f"ucl_ctx_lu_variant failed with code {v}")
+        return bool(v), float(a.value), float(b.value)
 
     # ---------------------------------------------------------------- #
     def rates(self, params: np.ndarray, abund: np.ndarray, av: np.ndarray, phi: np.ndarray):

@@ -145,7 +145,7 @@ __device__ int dv_jac(Ctx<T>& C) {
   // on this problem it multiplied Newton convergence failures, so the
   // factors are kept and applied by triangular solves.)
   const int info = block_lu<T>(C.W.P, n, C.W.perm, C.lu_smem, C.sh->si, C.W.scr, C.sh->lperm,
-                               sizeof(T) == 4 ? &C.sh->tc : nullptr);
+                               (sizeof(T) == 4 && C.N->lu_tc) ? &C.sh->tc : nullptr);
   lu_diag_inverses<T>(C.W.P, n, C.W.dinv, (T*)C.lu_smem);
   __syncthreads();
   ph_end(C.sh->ms, PH_LU);

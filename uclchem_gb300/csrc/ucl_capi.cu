@@ -264,6 +264,7 @@ struct DeviceTables {
   void* dbuf = nullptr;
   size_t bytes = 0;
   int nchunk = 0;
+  float lu_us_tc = 0.f, lu_us_cuda = 0.f;  // autotuner's FP32 LU timings (0: not measured)
 };
 
 static int build_tables(const ucl_network* net, const Consts& K, DeviceTables& T) {
@@ -744,6 +745,81 @@ static int max_slots(ucl_ctx* c) {
   return per_sm * c->nsm;
 }
 
+// LU-variant autotuner.  Per network, time the FP32 factorisation of a wave
+// of Newton-like test matrices (I - R, R random with column scales
+// 10^U(-3,1), a fixed seed) with the tensor-core and with the CUDA-core
+// trailing update, and keep the faster for that network's solves
+// (DevNet::lu_tc).  Networks above TC_MAX_N have only the CUDA-core update.
+// UCL_AUTOTUNE=0 in the environment skips the timing and keeps the tensor
+// cores wherever they apply.
+static int tune_lu(ucl_ctx* c, DeviceTables& t) {
+  const int n = t.dn.neq;
+  t.dn.lu_tc = LuSmem<float>::tc_ok(n) ? 1 : 0;
+  const char* env = getenv("UCL_AUTOTUNE");
+  if (!t.dn.lu_tc || (env && env[0] == '0')) return UCL_OK;
+  const int B = std::min(32, std::max(1, c->nsm));
+  const size_t nn = (size_t)n * n;
+  std::vector<float> h(nn * B);
+  uint64_t st = 0x9E3779B97F4A7C15ull ^ (uint64_t)n;
+  auto next = [&st]() {  // splitmix64
+    uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return (double)((z ^ (z >> 31)) >> 11) * (1.0 / 9007199254740992.0);
+  };
+  for (int b = 0; b < B; ++b) {
+    std::vector<double> cs(n);
+    for (int j = 0; j < n; ++j) cs[j] = pow(10.0, -3.0 + 4.0 * next());
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j)
+        h[b * nn + (size_t)i * n + j] = (float)((i == j ? 1.0 : 0.0) - (2.0 * next() - 1.0) * cs[j]);
+  }
+  float *src = nullptr, *work = nullptr, *scr = nullptr;
+  int *perm = nullptr, *info = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = UCL_E_CUDA;
+  const size_t sm = lu_smem_bytes<float>(n);
+  do {
+    if (cudaMalloc(&src, nn * B * 4) != cudaSuccess || cudaMalloc(&work, nn * B * 4) != cudaSuccess ||
+        cudaMalloc(&scr, (size_t)B * 2 * LuCfg<float>::NB * n * 4) != cudaSuccess ||
+        cudaMalloc(&perm, (size_t)B * n * 4) != cudaSuccess || cudaMalloc(&info, (size_t)B * 4) != cudaSuccess) {
+      rc = UCL_E_NOMEM;
+      break;
+    }
+    if (cudaMemcpy(src, h.data(), nn * B * 4, cudaMemcpyHostToDevice) != cudaSuccess) break;
+    if (cudaFuncSetAttribute(k_lu_batch<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+        cudaSuccess)
+      break;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) break;
+    float best[2] = {1e30f, 1e30f};
+    bool ok = true;
+    for (int rep = 0; rep < 3 && ok; ++rep)
+      for (int v = 0; v < 2 && ok; ++v) {  // v = 1: tensor cores
+        ok = cudaMemcpyAsync(work, src, nn * B * 4, cudaMemcpyDeviceToDevice, c->stream) == cudaSuccess &&
+             cudaEventRecord(e0, c->stream) == cudaSuccess;
+        k_lu_batch<float><<<B, NT, sm, c->stream>>>(work, n, perm, info, scr, B, v);
+        ok = ok && cudaGetLastError() == cudaSuccess && cudaEventRecord(e1, c->stream) == cudaSuccess &&
+             cudaEventSynchronize(e1) == cudaSuccess;
+        float ms = 0.f;
+        ok = ok && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
+        if (ok) best[v] = std::min(best[v], ms * 1e3f);
+      }
+    if (!ok) break;
+    t.lu_us_cuda = best[0];
+    t.lu_us_tc = best[1];
+    t.dn.lu_tc = best[1] <= best[0] ? 1 : 0;
+    rc = UCL_OK;
+  } while (false);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(src);
+  cudaFree(work);
+  cudaFree(scr);
+  cudaFree(perm);
+  cudaFree(info);
+  return rc;
+}
+
 static void ctx_free(ucl_ctx* c) {
   for (auto& t : c->tabs) cudaFree(t.dbuf);
   if (c->nets_d) cudaFree(c->nets_d);
@@ -780,6 +856,11 @@ static int ctx_create(const ucl_network* const* nets, int nnets, int device, siz
     c->njch = std::max(c->njch, c->tabs.back().dn.njch);
   }
   c->neq = c->nspec + 1;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { ctx_free(c); return UCL_E_CUDA; }
+  for (auto& t : c->tabs) {
+    const int rc = tune_lu(c, t);
+    if (rc != UCL_OK) { ctx_free(c); return rc; }
+  }
   std::vector<DevNet> dn;
   for (const auto& t : c->tabs) dn.push_back(t.dn);
   if (cudaMalloc(&c->nets_d, dn.size() * sizeof(DevNet)) != cudaSuccess) { ctx_free(c); return UCL_E_NOMEM; }
@@ -787,7 +868,6 @@ static int ctx_create(const ucl_network* const* nets, int nnets, int device, siz
     ctx_free(c);
     return UCL_E_CUDA;
   }
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { ctx_free(c); return UCL_E_CUDA; }
   c->smem32 = solver_smem<float>(c);
   c->smem64 = solver_smem<double>(c);
   c->slots_fp32 = max_slots<float>(c);
@@ -1346,4 +1426,12 @@ extern "C" int ucl_ctx_slots(const ucl_ctx* c, int precision) {
 }
 
 extern "C" int ucl_ctx_nspec(const ucl_ctx* c) { return c ? c->nspec : 0; }
+
+extern "C" int ucl_ctx_lu_variant(const ucl_ctx* c, int net, float* us_tensor, float* us_cuda) {
+  if (!c || net < 0 || net >= (int)c->tabs.size()) return UCL_E_ARG;
+  const DeviceTables& t = c->tabs[net];
+  if (us_tensor) *us_tensor = t.lu_us_tc;
+  if (us_cuda) *us_cuda = t.lu_us_cuda;
+  return t.dn.lu_tc;
+}
 extern "C" int ucl_ctx_nreac(const ucl_ctx* c) { return c ? c->nreac : 0; }

@@ -125,6 +125,9 @@ struct DevNet {
   int njch;                // chunks of <= 8 contributions (their partial sums
                            // go to a per-slot global buffer of njch doubles)
   int npart;               // max(nchunk, njch)
+  int lu_tc;               // FP32 LU trailing update on the tensor cores (1) or the
+                           // CUDA cores (0): chosen per network by the context's
+                           // autotuner (ucl_capi.cu tune_lu)
   const unsigned* jent;    // nchunks << 16 | first chunk
   const unsigned* jchunk;  // len << 16 | first contribution
   const unsigned* jcpack;  // (coef & 0xff) << 16 | key

@@ -557,14 +557,15 @@ __global__ void __launch_bounds__(NT, 1) k_solve_models(SolveIO io, SlotArrays<T
 // Batched dense LU (ucl_lu_factor_device): one CTA per matrix, the same
 // factorisation the solver applies to its Newton matrices.
 template <typename T>
-__global__ void __launch_bounds__(NT) k_lu_batch(T* mats, int n, int* perm, int* info, T* scr, int nsys) {
+__global__ void __launch_bounds__(NT) k_lu_batch(T* mats, int n, int* perm, int* info, T* scr, int nsys,
+                                                 int allow_tc = 1) {
   extern __shared__ __align__(16) char smem[];
   __shared__ int si[LU_SI_INTS];
   __shared__ int lperm[MAX_NEQ];
   __shared__ TcState tc;
   const int s = blockIdx.x;
   if (s >= nsys) return;
-  const bool use_tc = LuSmem<T>::tc_ok(n);
+  const bool use_tc = allow_tc && LuSmem<T>::tc_ok(n);
   if (use_tc) tc_setup(&tc, tc_cols_for(n));
   const int r = block_lu<T>(mats + (size_t)s * n * n, n, perm + (size_t)s * n, smem, si,
                             scr + (size_t)s * 2 * LuCfg<T>::NB * n, lperm, use_tc ? &tc : nullptr);
