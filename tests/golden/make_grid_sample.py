@@ -11,7 +11,10 @@ reference's rates + GETYDOT + DVODE MF=22 path) on a seeded sample of the
   the mixed-precision error statement.
 
 The runs take the oracle tens of CPU-minutes per slow model; they run in a
-process pool.  Usage: python tests/golden/make_grid_sample.py [--procs N]
+process pool, each capped in CPU time (2400 s at the reference's tolerance,
+1200 s for a truth run): a capped run is stored with the oracle's cap flag
+(-99) and no rows, and the tests skip it.
+Usage: python tests/golden/make_grid_sample.py [--procs N]
 """
 import argparse
 import multiprocessing as mp
@@ -27,6 +30,7 @@ sys.path.insert(0, ROOT)
 
 SEED = 20261203
 SAMPLE = 64
+CAP_S = {False: 2400.0, True: 1200.0}
 ROWS = 501
 FLOOR_MDEX = -16000
 
@@ -51,6 +55,7 @@ def run(task):
     if tight:
         p["reltol"] = 1e-12
         p["mxstep"] = 100000
+    _ORC.set_cpu_limit(CAP_S[tight])
     t = time.process_time()
     phys, ab, flag, cnt = _ORC.cloud(p, max_rows=ROWS)
     return i, tight, int(flag), len(phys), cnt, phys[:, 0].copy(), quantize(ab), time.process_time() - t

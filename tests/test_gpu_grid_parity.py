@@ -25,6 +25,7 @@ ROWS = 501
 # outliers"): index -> reason.  They must still succeed with the oracle's
 # rows; their dex bound is not applied.
 OUTLIERS = {}
+CAPPED = -99  # the oracle's run hit its CPU-time cap when the fixture was made: no reference result
 
 
 @pytest.fixture(scope="module")
@@ -74,6 +75,8 @@ def test_grid_sample_matches_oracle(runs, precision):
     ph, ab, nr, fl, st = out[precision]
     bad = []
     for k, i in enumerate(fx["index"]):
+        if fx["flag"][k] == CAPPED:
+            continue
         assert fl[k] == fx["flag"][k], (int(i), fl[k], fx["flag"][k])
         assert nr[k] == fx["nrows"][k], (int(i), nr[k], fx["nrows"][k])
         oab, otyr = _oracle_rows(fx, k)
