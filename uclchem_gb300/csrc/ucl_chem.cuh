@@ -397,6 +397,18 @@ struct RhsScal {
   int sm_on, blr_on, neg;
 };
 
+// A small integer coefficient (|c| < 2^20) as a double, built from its bits
+// on the integer pipe: the same value as (double)c, without the FP64
+// conversion (on this GPU the FP64 pipe issues a warp instruction in many
+// cycles, and the RHS gather has one coefficient per term).
+__device__ __forceinline__ double coef_to_double(int c) {
+  const unsigned a = c < 0 ? (unsigned)(-c) : (unsigned)c;
+  const int e = 31 - __clz(a);  // floor(log2 a) for a > 0
+  unsigned hi = ((unsigned)(1023 + e) << 20) | ((a << (20 - e)) & 0xFFFFFu);
+  hi = a ? (hi | (c < 0 ? 0x80000000u : 0u)) : 0u;
+  return __hiloint2double((int)hi, 0);
+}
+
 // flux of reaction r for the current scalars (shape-8 needs R.ts)
 __device__ __forceinline__ double flux_of(int sh, double k, double D, double ya, double yb, const RhsScal& R) {
   switch (sh) {
@@ -523,7 +535,7 @@ __device__ void dev_rhs(const DevNet& N, const ucl_model_params& P, const SysPhy
       double s = 0.0;
 #pragma unroll
       for (int j = 0; j < CHMAX; ++j)
-        if (j < len) s += (double)(signed char)(e[u][j] >> 16) * flux[e[u][j] & 0xFFFFu];
+        if (j < len) s += coef_to_double((signed char)(e[u][j] >> 16)) * flux[e[u][j] & 0xFFFFu];
       if (c0 + u * NT < N.nchunk) part[c0 + u * NT] = s;
     }
   }
@@ -658,7 +670,7 @@ __device__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhy
             case 3: d = flux[r] * dsm; break;
             default: d = flux[r] * dblr; break;
           }
-          v += (double)(signed char)(e[u][j] >> 16) * d;
+          v += coef_to_double((signed char)(e[u][j] >> 16)) * d;
         }
       }
       if (c0 + u * NT < N.njch) jpart[c0 + u * NT] = v;
