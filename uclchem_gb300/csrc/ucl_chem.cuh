@@ -409,6 +409,11 @@ __device__ __forceinline__ double coef_to_double(int c) {
   return __hiloint2double((int)hi, 0);
 }
 
+// barrier of the `count` threads (a multiple of 32) that use named barrier `id`
+__device__ __forceinline__ void bar_sync_named(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
 // flux of reaction r for the current scalars (shape-8 needs R.ts)
 __device__ __forceinline__ double flux_of(int sh, double k, double D, double ya, double yb, const RhsScal& R) {
   switch (sh) {
@@ -472,10 +477,18 @@ __device__ void dev_rhs(const DevNet& N, const ucl_model_params& P, const SysPhy
       }
     }
   } else {
+    // warps 2..: the reaction fluxes, the surface-swap fluxes, the CSR
+    // gather and the row sums, while warps 0 and 1 evaluate the
+    // self-shielded photo rates.  The two photo reactions' terms are left
+    // out here and added to their rows once the rates are known, so the
+    // photo evaluation is off this critical path.  The warps synchronise on
+    // named barrier 1 (NTF threads).
+    constexpr int NTF = NT - 64;
+    const int t = tid - 64;
+    const int rh = N.rx_h2hv, rc = N.rx_cohv;
     // U reactions per thread per round, all table and rate loads first
     constexpr int U = 9;
-    constexpr int NTF = NT - 64;
-    for (int r0 = tid - 64; r0 < N.nreac; r0 += U * NTF) {
+    for (int r0 = t; r0 < N.nreac; r0 += U * NTF) {
       unsigned pk[U];
       double kk[U];
 #pragma unroll
@@ -488,65 +501,69 @@ __device__ void dev_rhs(const DevNet& N, const ucl_model_params& P, const SysPhy
       for (int u = 0; u < U; ++u) {
         const int r = r0 + u * NTF;
         const int sh = (int)(pk[u] >> 28);
-        if (r < N.nreac && sh != SH_Y_TS_SM) {
+        if (r < N.nreac && sh != SH_Y_TS_SM && r != rh && r != rc) {
           const int ya = (int)(pk[u] & 0x3FFFu), yb = (int)((pk[u] >> 14) & 0x3FFFu) - 1;
           flux[r] = flux_of(sh, kk[u], D, y[ya], yb >= 0 ? y[yb] : 0.0, R);
         }
       }
     }
-  }
-  __syncthreads();
-  // photo fluxes, totalSwap and the surface-swap fluxes (warp 0)
-  if (warp == 0) {
-    if (lane == 0 && N.rx_h2hv >= 0)
-      flux[N.rx_h2hv] = flux_of(N.fshape[N.rx_h2hv], R.kh2, D, y[N.fya[N.rx_h2hv]],
-                                N.fyb[N.rx_h2hv] >= 0 ? y[N.fyb[N.rx_h2hv]] : 0.0, R);
-    if (lane == 0 && N.rx_cohv >= 0)
-      flux[N.rx_cohv] = flux_of(N.fshape[N.rx_cohv], R.kco, D, y[N.fya[N.rx_cohv]],
-                                N.fyb[N.rx_cohv] >= 0 ? y[N.fyb[N.rx_cohv]] : 0.0, R);
-    double s = 0.0;
-    for (int r = N.swap_lo + lane; r < N.swap_hi; r += 32) s += flux[r];
-    s = warp_sum(s);
-    RhsScal L = R;
-    L.ts = s;
-    if (lane == 0) R.ts = s;
-    for (int k = lane; k < N.n_ts; k += 32) {
-      const int r = N.ts_rx[k];
-      flux[r] = flux_of(SH_Y_TS_SM, rate[r], D, y[N.fya[r]], 0.0, L);
+    bar_sync_named(1, NTF);
+    // totalSwap and the surface-swap fluxes (warp 2)
+    if (warp == 2) {
+      double sw = 0.0;
+      for (int r = N.swap_lo + lane; r < N.swap_hi; r += 32) sw += flux[r];
+      sw = warp_sum(sw);
+      if (lane == 0) R.ts = sw;
+      for (int k = lane; k < N.n_ts; k += 32) {
+        const int r = N.ts_rx[k];
+        flux[r] = rate[r] * y[N.fya[r]] * sw * R.ism;  // RATE*Y*totalSwap/safeMantle
+      }
     }
-  }
-  __syncthreads();
-  // chunked CSR gather: two chunks per thread per round, the <= 2 x 12
-  // entry words loaded before any flux is read
-  constexpr int CHMAX = 12;
-  for (int c0 = tid; c0 < N.nchunk; c0 += 2 * NT) {
-    unsigned cp[2], e[2][CHMAX];
+    bar_sync_named(1, NTF);
+    // chunked CSR gather: two chunks per thread per round, the <= 2 x 12
+    // entry words loaded before any flux is read (photo terms skipped)
+    constexpr int CHMAX = 12;
+    for (int c0 = t; c0 < N.nchunk; c0 += 2 * NTF) {
+      unsigned cp[2], e[2][CHMAX];
 #pragma unroll
-    for (int u = 0; u < 2; ++u) cp[u] = c0 + u * NT < N.nchunk ? N.chpack[c0 + u * NT] : 0u;
+      for (int u = 0; u < 2; ++u) cp[u] = c0 + u * NTF < N.nchunk ? N.chpack[c0 + u * NTF] : 0u;
 #pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      const int beg = (int)(cp[u] & 0xFFFFu), len = (int)((cp[u] >> 16) & 0xFu);
+      for (int u = 0; u < 2; ++u) {
+        const int beg = (int)(cp[u] & 0xFFFFu), len = (int)((cp[u] >> 16) & 0xFu);
 #pragma unroll
-      for (int j = 0; j < CHMAX; ++j) e[u][j] = j < len ? N.stpack[beg + j] : 0u;
+        for (int j = 0; j < CHMAX; ++j) e[u][j] = j < len ? N.stpack[beg + j] : 0u;
+      }
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int len = (int)((cp[u] >> 16) & 0xFu);
+        double s = 0.0;
+#pragma unroll
+        for (int j = 0; j < CHMAX; ++j) {
+          const int r = (int)(e[u][j] & 0xFFFFu);
+          if (j < len && r != rh && r != rc) s += coef_to_double((signed char)(e[u][j] >> 16)) * flux[r];
+        }
+        if (c0 + u * NTF < N.nchunk) part[c0 + u * NTF] = s;
+      }
     }
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      const int len = (int)((cp[u] >> 16) & 0xFu);
+    bar_sync_named(1, NTF);
+    // row sums of the chunk partials, in chunk order (rows without terms: 0)
+    for (int i = t; i < N.neq; i += NTF) {
+      const unsigned rw = N.rowch[i];
+      const int c = (int)(rw & 0xFFFFu), cnt = (int)(rw >> 16);
       double s = 0.0;
-#pragma unroll
-      for (int j = 0; j < CHMAX; ++j)
-        if (j < len) s += coef_to_double((signed char)(e[u][j] >> 16)) * flux[e[u][j] & 0xFFFFu];
-      if (c0 + u * NT < N.nchunk) part[c0 + u * NT] = s;
+      for (int k = 0; k < cnt; ++k) s = k == 0 ? part[c] : s + part[c + k];
+      ydot[i] = s;
     }
   }
+  // the photo fluxes (RATE*Y, checked when the tables are built), from the
+  // warps that evaluated the rates
+  if (tid == 0 && N.rx_cohv >= 0) flux[N.rx_cohv] = R.kco * y[N.fya[N.rx_cohv]];
+  if (tid == 32 && N.rx_h2hv >= 0) flux[N.rx_h2hv] = R.kh2 * y[N.fya[N.rx_h2hv]];
   __syncthreads();
-  // row sums of the chunk partials, in chunk order (rows without terms: 0)
-  for (int i = tid; i < N.neq; i += NT) {
-    const unsigned rc = N.rowch[i];
-    const int c = (int)(rc & 0xFFFFu), cnt = (int)(rc >> 16);
-    double s = 0.0;
-    for (int k = 0; k < cnt; ++k) s = k == 0 ? part[c] : s + part[c + k];
-    ydot[i] = s;
+  // their terms in the rows of the species they touch
+  if (tid < N.n_ph) {
+    const double fh = N.rx_h2hv >= 0 ? flux[N.rx_h2hv] : 0.0, fc = N.rx_cohv >= 0 ? flux[N.rx_cohv] : 0.0;
+    ydot[N.ph_row[tid]] += (double)N.ph_c1[tid] * fh + (double)N.ph_c2[tid] * fc;
   }
   __syncthreads();
   // surface <-> bulk transfer (odes.f90:4815-5180)
