@@ -130,13 +130,13 @@ def element_drift(tot: np.ndarray, nrows: np.ndarray, flags: np.ndarray) -> floa
 
 
 def full_grid_conservation(ab_d, nrows, flags, dev):
-    """Largest relative drift of the H, He, C, N, O and S totals over every
-    output row of every successful model (totals formed on the device)."""
+    """Largest relative drift of the network's conserved element totals (He,
+    C, N, O, S, Si, Mg, Cl: every element each reaction conserves; H is not,
+    some freeze-outs hydrogenate) over every output row of every successful
+    model (totals formed on the device)."""
     import torch
     from uclchem_gb300 import network
-    from uclchem_gb300.analysis import element_counts
-    species = network.load_default().species
-    E = np.stack([element_counts(species, e) for e in ("H", "HE", "C", "N", "O", "S")], axis=1)
+    E = network.load_default().invariants().T
     Ed = torch.from_numpy(E.astype(np.float64)).to(dev)
     tot = np.concatenate([torch.matmul(ab_d[i:i + 256], Ed).cpu().numpy() for i in range(0, ab_d.shape[0], 256)])
     return element_drift(tot, nrows, flags)

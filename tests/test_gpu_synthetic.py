@@ -93,4 +93,5 @@ def test_four_network_sizes_in_one_launch_match_oracle(setup, precision):
         scale = np.abs(y[0]) @ np.abs(E).T
         worst_drift = max(worst_drift, float((np.abs(tot - tot[0]) / scale).max()))
     assert worst_dex < 0.01, worst_dex
-    assert worst_drift < (1e-9 if precision == 0 else 1e-8), worst_drift
+    # FP64: the DVODE iteration as is; mixed: projected onto the invariants
+    assert worst_drift < (1e-9 if precision == 0 else 1e-10), worst_drift

@@ -121,3 +121,21 @@ def test_grid_parameters_are_seeded_and_in_range():
     # log-uniform: about a fifth of the points per decade of density
     counts = np.histogram(np.log10(dens), bins=5, range=(2, 7))[0]
     assert (np.abs(counts / 4096 - 0.2) < 0.03).all()
+
+
+def test_invariants_are_exactly_conserved_by_every_reaction(net):
+    """The linear invariants the mixed path projects onto: element counts
+    that every reaction conserves (integer check over the stoichiometry).
+    H is not among them: a few freeze-outs hydrogenate (C2N -> #CH3CNH)."""
+    from uclchem_gb300.analysis import element_counts
+    inv = net.invariants()
+    S = np.zeros((net.nspec, net.nreac), dtype=np.int64)
+    for i in range(net.nspec):
+        for e in range(net.stoich_ptr[i], net.stoich_ptr[i + 1]):
+            S[i, net.stoich_rx[e]] += net.stoich_coef[e]
+    assert inv.shape == (8, net.nspec)
+    assert not (inv @ S).any()
+    h = element_counts(net.species, "H")
+    assert (h @ S).any()
+    for el in ("HE", "C", "N", "O", "S", "SI", "MG", "CL"):
+        assert any((row == element_counts(net.species, el)).all() for row in inv), el

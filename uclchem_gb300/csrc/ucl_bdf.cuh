@@ -55,6 +55,7 @@ struct Shared {
   int si[LU_SI_INTS];
   int lperm[MAX_NEQ];
   TcState tc;
+  double inv_g[MAX_INV], inv_l[MAX_INV];  // invariant residues and multipliers
 };
 
 // per-CTA workspace (global memory)
@@ -68,6 +69,7 @@ struct Slot {
   T* scr;        // [2*NB*n] row-interchange staging
   T* dinv;       // [ceil(n/32) * 2 * 1024] inverses of the diagonal blocks of L and U
   double* jpart; // [njch] partial sums of the Jacobian's entry chunks
+  double* ginv;  // [n_inv * n_inv] inverse Gram matrix of the invariants (mixed path)
 };
 
 template <typename T>
@@ -119,6 +121,138 @@ __device__ __forceinline__ void rhs(Ctx<T>& C, const double* y, double* out, boo
   ph_end(C.sh->ms, PH_RHS);
 }
 
+// ---------------------------------------------------------------------------
+// Conservative projection of the mixed path's Newton corrections.  Every
+// reaction conserves the network's invariants c (element counts), so c.f = 0
+// and c.J = 0, hence c.P = c for P = I - h*rl1*J and the exact Newton
+// correction keeps c.acor = 0: each step conserves the invariants to FP64
+// rounding, as the reference's FP64 solve does.  The FP32 factors satisfy
+// c.(P~^-1 r) = c.r only to the FP32 solve's error, amplified by cond(P~),
+// and over ~10^6 steps the residue adds up (1e-5 relative drift measured).
+// At convergence the mixed path therefore removes the invariant component:
+//   acor <- acor - Q C (C^T Q C)^-1 C^T acor,   Q = diag(1/ewt^2),
+// the smallest change of acor in DVODE's weighted norm with C^T acor = 0.
+// G = C^T Q C is formed and inverted at each Jacobian evaluation (with the
+// error weights of that moment), so a step pays two short reductions.
+
+// G and its inverse (Jacobi-scaled Gauss-Jordan, SPD: no pivoting) into
+// W.ginv; an invariant whose scaled pivot vanishes voids the projection
+// until the next Jacobian (G^-1 = 0).  All threads call.
+template <typename T>
+__device__ void inv_prepare(Ctx<T>& C) {
+  const DevNet& N = *C.N;
+  const int E = N.n_inv, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int E2 = 2 * E;
+  double* A = reinterpret_cast<double*>(C.lu_smem);  // [E][2E] scratch: the LU area is idle here
+  const int npair = E * (E + 1) / 2;
+  for (int p = warp; p < npair; p += NWARP) {
+    int e = 0, rem = p;
+    while (rem >= E - e) { rem -= E - e; ++e; }
+    const int f = e + rem;
+    double acc = 0.0;
+    for (int k = N.inv_el_ptr[e] + lane; k < N.inv_el_ptr[e + 1]; k += 32) {
+      const unsigned w = N.inv_el[k];
+      const int sp = (int)(w >> 8), ce = (int)(signed char)(w & 0xFFu);
+      int cf = 0;
+      for (int q = N.inv_sp_ptr[sp]; q < N.inv_sp_ptr[sp + 1]; ++q) {
+        const unsigned v = N.inv_sp[q];
+        if ((int)(v >> 8) == f) cf = (int)(signed char)(v & 0xFFu);
+      }
+      if (cf) {
+        const double qs = C.wJi[sp] * C.wJi[sp];
+        acc += qs * coef_to_double(ce * cf);
+      }
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) {
+      A[e * E2 + f] = acc;
+      A[f * E2 + e] = acc;
+    }
+  }
+  __syncthreads();
+  if (warp == 0) {
+    // lane j: column j of the scaled G and column E + j of the identity
+    const double gjj = lane < E ? A[lane * E2 + lane] : 1.0;
+    const double dj = gjj > 0.0 ? 1.0 / sqrt(gjj) : 0.0;
+    bool ok = __all_sync(0xffffffffu, lane >= E || gjj > 0.0);
+    for (int i = 0; i < E; ++i) {
+      const double di = __shfl_sync(0xffffffffu, dj, i);
+      if (lane < E) {
+        A[i * E2 + lane] = A[i * E2 + lane] * di * dj;
+        A[i * E2 + E + lane] = (i == lane) ? 1.0 : 0.0;
+      }
+    }
+    __syncwarp();
+    for (int k = 0; k < E && ok; ++k) {
+      const double piv = A[k * E2 + k];
+      ok = piv > 1e-10;
+      if (!ok) break;
+      __syncwarp();
+      const double ip = 1.0 / piv;
+      if (lane < E) {
+        A[k * E2 + lane] *= ip;
+        A[k * E2 + E + lane] *= ip;
+      }
+      __syncwarp();
+      for (int i = 0; i < E; ++i) {
+        if (i == k) continue;
+        const double fct = A[i * E2 + k];
+        __syncwarp();
+        if (lane < E) {
+          A[i * E2 + lane] -= fct * A[k * E2 + lane];
+          A[i * E2 + E + lane] -= fct * A[k * E2 + E + lane];
+        }
+        __syncwarp();
+      }
+    }
+    // G^-1 = D (DGD)^-1 D
+    for (int i = 0; i < E; ++i) {
+      const double di = __shfl_sync(0xffffffffu, dj, i);
+      if (lane < E) C.W.ginv[i * E + lane] = ok ? di * A[i * E2 + E + lane] * dj : 0.0;
+    }
+  }
+  __syncthreads();
+}
+
+// acor <- acor - Q C G^-1 C^T acor and y = yh + acor.  All threads call.
+template <typename T>
+__device__ void inv_project(Ctx<T>& C) {
+  const DevNet& N = *C.N;
+  Shared& sh = *C.sh;
+  const int E = N.n_inv, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, n = C.n;
+  for (int e = warp; e < E; e += NWARP) {
+    double s = 0.0;
+    for (int k = N.inv_el_ptr[e] + lane; k < N.inv_el_ptr[e + 1]; k += 32) {
+      const unsigned w = N.inv_el[k];
+      s += coef_to_double((signed char)(w & 0xFFu)) * C.acor[w >> 8];
+    }
+    s = warp_sum(s);
+    if (lane == 0) sh.inv_g[e] = s;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    double l = 0.0;
+    if (lane < E)
+      for (int f = 0; f < E; ++f) l += C.W.ginv[lane * E + f] * sh.inv_g[f];
+    if (lane < E) sh.inv_l[lane] = l;
+  }
+  __syncthreads();
+  const double* yh = C.W.yh;
+  for (int i = tid; i < n; i += NT) {
+    const int b = N.inv_sp_ptr[i], e1 = N.inv_sp_ptr[i + 1];
+    if (b == e1) continue;
+    double s = 0.0;
+    for (int q = b; q < e1; ++q) {
+      const unsigned v = N.inv_sp[q];
+      s += coef_to_double((signed char)(v & 0xFFu)) * sh.inv_l[v >> 8];
+    }
+    const double a = C.acor[i] - C.wJi[i] * C.wJi[i] * s;
+    C.acor[i] = a;
+    C.y[i] = yh[i] + a;
+  }
+  __syncthreads();
+}
+
 // DVJAC (MITER=2 decision logic, analytic J) + P = I - h*rl1*J + LU
 template <typename T>
 __device__ int dv_jac(Ctx<T>& C) {
@@ -131,6 +265,9 @@ __device__ int dv_jac(Ctx<T>& C) {
     ph_begin(C.sh->ms);
     dev_jac<(sizeof(T) == 4), T>(*C.N, C.sh->P, C.sh->S, C.y, C.W.rate, C.wJ, C.wJi, C.W.J, C.flux, C.dfa,
                                  C.dfb, C.vec, C.W.jpart, C.sh->R);
+    if constexpr (sizeof(T) == 4) {
+      if (C.N->n_inv > 0) inv_prepare<T>(C);
+    }
     ph_end(C.sh->ms, PH_JAC);
   } else {
     if (tid == 0) d.jcur = 0;
@@ -232,6 +369,9 @@ __device__ int dv_nlsd(Ctx<T>& C, int nflag) {
       }
       __syncthreads();
       if (d.nls_out == 0) {
+        if constexpr (sizeof(T) == 4) {
+          if (C.N->n_inv > 0) inv_project<T>(C);
+        }
         const double acn = (d.m == 0) ? d.del : bnorm(C.acor, C.ewt, n, C.sh->red);
         if (tid == 0) { d.jcur = 0; d.icf = 0; d.acnrm = acn; }
         __syncthreads();

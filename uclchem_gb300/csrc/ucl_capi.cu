@@ -453,6 +453,33 @@ static int build_tables(const ucl_network* net, const Consts& K, DeviceTables& T
     if (i < 0 || i >= ns) return UCL_E_NET;
   D.n_ion = (int)ions.size();
   D.n_refr = (int)refr.size();
+  // linear invariants [E][nspec] (older blobs: none, no projection)
+  std::vector<int> isp_ptr(n + 1, 0), iel_ptr(1, 0);
+  std::vector<unsigned> isp, iel;
+  if (net->ints.count("inv_counts")) {
+    const auto& ic = net->I("inv_counts");
+    if (ic.size() % ns != 0) return UCL_E_NET;
+    const int E = (int)(ic.size() / ns);
+    if (E <= MAX_INV) {
+      for (int e = 0; e < E; ++e) {
+        for (int i = 0; i < ns; ++i) {
+          const int cnt = ic[(size_t)e * ns + i];
+          if (cnt < -128 || cnt > 127) return UCL_E_NET;
+          if (cnt) iel.push_back((unsigned)i << 8 | ((unsigned)cnt & 0xFFu));
+        }
+        iel_ptr.push_back((int)iel.size());
+      }
+      for (int i = 0; i < ns; ++i) {
+        for (int e = 0; e < E; ++e) {
+          const int cnt = ic[(size_t)e * ns + i];
+          if (cnt) isp.push_back((unsigned)e << 8 | ((unsigned)cnt & 0xFFu));
+        }
+        isp_ptr[i + 1] = (int)isp.size();
+      }
+      isp_ptr[n] = (int)isp.size();
+      D.n_inv = E;
+    }
+  }
   D.n_fp = (int)fp.size();
   D.desoh2_1 = first_of(R_DESOH2); D.descr_1 = first_of(R_DESCR); D.deuvcr_1 = first_of(R_DEUVCR);
   D.therm_1 = first_of(R_THERM);
@@ -662,6 +689,10 @@ static int build_tables(const ucl_network* net, const Consts& K, DeviceTables& T
   img.add(D.ar_coef, ar_coef);
   img.add(D.ion_list, ions);
   img.add(D.refr_list, refr);
+  img.add(D.inv_sp_ptr, isp_ptr);
+  img.add(D.inv_sp, isp);
+  img.add(D.inv_el_ptr, iel_ptr);
+  img.add(D.inv_el, iel);
   img.add(D.ph_row, ph_row);
   img.add(D.ph_c1, ph_c1);
   img.add(D.ph_c2, ph_c2);
@@ -715,7 +746,8 @@ struct ucl_ctx {
 template <typename T>
 static size_t slot_bytes(int n, int nreac, int njch) {
   return (size_t)nreac * 8 + 2 * mat_stride(n) * sizeof(T) + (size_t)n * 4 +
-         (size_t)2 * LuCfg<T>::NB * n * sizeof(T) + dinv_elems(n) * sizeof(T) + (size_t)njch * 8 + 6 * 256;
+         (size_t)2 * LuCfg<T>::NB * n * sizeof(T) + dinv_elems(n) * sizeof(T) + (size_t)njch * 8 +
+         (size_t)MAX_INV * MAX_INV * 8 + 7 * 256;
 }
 
 template <typename T>
@@ -926,9 +958,10 @@ static int solve_dev(ucl_ctx* c, DevBuf& wsbuf, const SolveIO& io, int nslots_re
                j_b = a256((size_t)nslots * mat_stride(n) * sizeof(T)), perm_b = a256((size_t)nslots * n * 4),
                scr_b = a256((size_t)nslots * 2 * LuCfg<T>::NB * n * sizeof(T)),
                dinv_b = a256((size_t)nslots * dinv_elems(n) * sizeof(T)),
-               jp_b = a256((size_t)nslots * c->njch * 8);
+               jp_b = a256((size_t)nslots * c->njch * 8),
+               gi_b = a256((size_t)nslots * MAX_INV * MAX_INV * 8);
   const size_t order_b = a256((size_t)nmodels * 4);
-  int rc = wsbuf.ensure(yh_b + rate_b + 2 * j_b + perm_b + scr_b + dinv_b + jp_b + 512 + order_b);
+  int rc = wsbuf.ensure(yh_b + rate_b + 2 * j_b + perm_b + scr_b + dinv_b + jp_b + gi_b + 512 + order_b);
   if (rc) return rc;
   char* base = (char*)wsbuf.p;
   SlotArrays<T> A;
@@ -940,10 +973,11 @@ static int solve_dev(ucl_ctx* c, DevBuf& wsbuf, const SolveIO& io, int nslots_re
   A.scr = (T*)(base + yh_b + rate_b + 2 * j_b + perm_b);
   A.dinv = (T*)(base + yh_b + rate_b + 2 * j_b + perm_b + scr_b);
   A.jpart = (double*)(base + yh_b + rate_b + 2 * j_b + perm_b + scr_b + dinv_b);
+  A.ginv = (double*)(base + yh_b + rate_b + 2 * j_b + perm_b + scr_b + dinv_b + jp_b);
   A.n = n;
   A.nreac = c->nreac;
   A.njch = c->njch;
-  int* counter = (int*)(base + yh_b + rate_b + 2 * j_b + perm_b + scr_b + dinv_b + jp_b);
+  int* counter = (int*)(base + yh_b + rate_b + 2 * j_b + perm_b + scr_b + dinv_b + jp_b + gi_b);
   unsigned long long* epoch = (unsigned long long*)((char*)counter + 16);
   int* order = (int*)((char*)counter + 512);
   if (cudaMemsetAsync(counter, 0, 32, st) != cudaSuccess) return UCL_E_CUDA;

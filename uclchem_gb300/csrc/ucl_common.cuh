@@ -21,6 +21,7 @@ constexpr int NT = UCL_NT;       // threads per CTA of the solver kernels
 constexpr int NWARP = NT / 32;
 constexpr int MAX_NEQ = 520;     // largest NEQ the kernels are compiled for
 constexpr int LMAXP = 7;         // Nordsieck columns held (MAXORD+2)
+constexpr int MAX_INV = 32;      // most linear invariants the mixed path projects onto
 // doubles of the Jacobian's vector scratch: [0, 256) per-row/ice
 // coefficients, [256, 512) their scaled copies, [512, 512 + NEQ) one staged
 // matrix row
@@ -65,6 +66,16 @@ struct DevNet {
   // refractory ice species subtracted from safeBulk at interval start
   int n_refr;
   const int* refr_list;
+  // linear invariants of the ODE system (element counts every reaction
+  // conserves), for the mixed path's projection of its Newton corrections:
+  // species-major entries inv_sp[inv_sp_ptr[i] ..] = invariant << 8 | count,
+  // invariant-major entries inv_el[inv_el_ptr[e] ..] = species << 8 | count
+  // (count as int8); n_inv = 0 switches the projection off
+  int n_inv;
+  const int* inv_sp_ptr;
+  const unsigned* inv_sp;
+  const int* inv_el_ptr;
+  const unsigned* inv_el;
   // ---- rates ----
   const uint8_t* rtype;
   const uint8_t* iceflag;  // PHOTON/CRPHOT: 1 surface, 2 bulk reactant; LHDES/ERDES: 1 bulk reactant

@@ -383,6 +383,7 @@ struct SlotArrays {
   T* scr;
   T* dinv;
   double* jpart;
+  double* ginv;
   int n, nreac, njch;
 };
 
@@ -398,6 +399,7 @@ __device__ __forceinline__ Slot<T> slot_of(const SlotArrays<T>& A, int s) {
   W.scr = A.scr + (size_t)s * 2 * LuCfg<T>::NB * n;
   W.dinv = A.dinv + (size_t)s * dinv_elems(n);
   W.jpart = A.jpart + (size_t)s * A.njch;
+  W.ginv = A.ginv + (size_t)s * MAX_INV * MAX_INV;
   return W;
 }
 

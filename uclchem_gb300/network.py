@@ -272,10 +272,36 @@ class Network:
     stoich_ptr: np.ndarray = field(default=None)   # CSR over species rows
     stoich_rx: np.ndarray = field(default=None)
     stoich_coef: np.ndarray = field(default=None)
+    # linear invariants of the ODE system, [E, nspec] integer weights (None:
+    # derived from the species names, see invariants())
+    invariant_counts: np.ndarray = field(default=None)
 
     @property
     def neq(self) -> int:
         return self.nspec + 1
+
+    def invariants(self) -> np.ndarray:
+        """[E, nspec] integer weight vectors c with c . ydot = 0 for every
+        reaction: the element counts (species-name counting of
+        uclchem_gb300.analysis) of every element that each reaction conserves
+        exactly.  An element that some reaction does not conserve (the
+        default network's freeze-outs that hydrogenate, e.g. C2N -> #CH3CNH)
+        is left out."""
+        if self.invariant_counts is not None:
+            return np.asarray(self.invariant_counts, dtype=np.int64).reshape(-1, self.nspec)
+        from .analysis import ELEMENTS, element_counts
+        S = np.zeros((self.nspec, self.nreac), dtype=np.int64)
+        for i in range(self.nspec):
+            for e in range(self.stoich_ptr[i], self.stoich_ptr[i + 1]):
+                S[i, self.stoich_rx[e]] += self.stoich_coef[e]
+        rows = []
+        for el in ELEMENTS:
+            if el in ("SURFACE", "BULK"):
+                continue
+            c = element_counts(self.species, el)
+            if c.any() and not (c @ S).any():
+                rows.append(c)
+        return np.array(rows, dtype=np.int64).reshape(-1, self.nspec)
 
     # ------------------------------------------------------------------ #
     def derive_flux_form(self) -> None:
@@ -395,6 +421,8 @@ class Network:
         add("stoich_coef", self.stoich_coef, 1)
         # positive ions for enforceChargeConservation (chemistry.f90:114-121)
         add("ion_list", [i for i, name in enumerate(self.species) if "+" in name], 1)
+        # linear invariants (conserved element counts), [E, nspec]
+        add("inv_counts", self.invariants(), 1)
         return _BLOB_MAGIC + b"".join(recs)
 
 

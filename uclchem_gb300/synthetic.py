@@ -230,6 +230,7 @@ def to_network(net: SyntheticNetwork):
     out.stoich_ptr = np.ascontiguousarray(net.stoich_ptr, dtype=np.int32)
     out.stoich_rx = np.ascontiguousarray(net.stoich_rx, dtype=np.int32)
     out.stoich_coef = np.ascontiguousarray(net.stoich_coef, dtype=np.int32)
+    out.invariant_counts = net.conserved()  # H, C, O, N counts and the charge
     return out
 
 
