@@ -106,9 +106,8 @@ template <typename T>
 __device__ void lin_solve(Ctx<T>& C, double* y) {
   const int n = C.n;
   ph_begin(C.sh->ms);
-  if constexpr (sizeof(T) == 4)  // the LU's shared area is idle during solves: stage blocks there
-    block_lusolve<T>(C.W.P, n, C.W.perm, C.W.dinv, y, C.wJ, C.wJi, C.xt, (T*)C.lu_smem,
-                     (T*)(C.lu_smem + 256), lu_smem_bytes<T>(n) - 256);
+  if constexpr (sizeof(T) == 4)
+    block_lusolve<T>(C.W.P, n, C.W.perm, C.W.dinv, y, C.wJ, C.wJi, C.xt, (T*)C.lu_smem);
   else
     block_lusolve<T>(C.W.P, n, C.W.perm, C.W.dinv, y, nullptr, nullptr, C.xt, (T*)C.lu_smem);
   ph_end(C.sh->ms, PH_SOLVE);

@@ -595,63 +595,22 @@ __device__ void lu_diag_inverses(const T* __restrict__ A, int n, T* __restrict__
 // The right-hand side comes in and the solution goes out as FP64 y (shared):
 // the system solved is (LU) x = W y and y <- W^-1 x, with W = diag(ws) and
 // W^-1 = diag(wis) (both nullptr: no scaling).
-// pre: shared staging of pre_bytes for the off-diagonal row blocks.  With
-// room for two 32 x n blocks (and 16-byte rows: n % 4 == 0), the block row
-// of the next step is copied into shared memory with cp.async while the
-// current step runs, so each step reads its matrix block from shared memory
-// instead of waiting for L2.
-__device__ __forceinline__ void cp_async16(void* dst_smem, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst_smem)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-
 template <typename T>
 __device__ void block_lusolve(const T* __restrict__ A, int n, const int* __restrict__ perm,
                               const T* __restrict__ dinv, double* y, const double* ws, const double* wis, T* tmp,
-                              T* rbuf, T* pre = nullptr, size_t pre_bytes = 0) {
+                              T* rbuf) {
   using V = typename Vec2<T>::type;
   constexpr int W = Vec2<T>::W;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nblk = (n + 31) / 32;
   const bool vec = (n % W) == 0;
-  // prefetched off-diagonal blocks: the t-th step (t < nblk forward, then
-  // backward) uses rows [k0, k0+nb) x columns [c0, c1) staged row by row with
-  // stride c1 - c0 in buffer t & 1
-  const bool use_pre = pre != nullptr && (n % 4) == 0 && ((uintptr_t)A & 15) == 0 &&
-                       pre_bytes >= (size_t)2 * 32 * n * sizeof(T);
-  auto seg = [&](int t, int& k0, int& nb, int& c0, int& c1) {
-    const int pass = t >= nblk, step = pass ? t - nblk : t;
-    const int b = pass == 0 ? step : nblk - 1 - step;
-    k0 = b * 32;
-    nb = min(32, n - k0);
-    c0 = pass == 0 ? 0 : k0 + nb;
-    c1 = pass == 0 ? k0 : n;
-  };
-  auto prefetch = [&](int t) {
-    int k0, nb, c0, c1;
-    seg(t, k0, nb, c0, c1);
-    const int q4 = (c1 - c0) / 4;  // 16-byte chunks per row (c0, c1 multiples of 4)
-    T* dst = pre + (size_t)(t & 1) * 32 * n;
-    for (int q = tid; q < nb * q4; q += NT) {
-      const int r = q / q4, cc = q - r * q4;
-      cp_async16(dst + (size_t)r * (c1 - c0) + 4 * cc, A + (size_t)(k0 + r) * n + c0 + 4 * cc);
-    }
-    cp_async_commit();
-  };
-  if (use_pre) prefetch(0);
   for (int i = tid; i < n; i += NT) {
     const int p = perm[i];
     tmp[i] = (T)(ws ? ws[p] * y[p] : y[p]);
   }
-  if (use_pre) cp_async_wait_all();
   __syncthreads();
   for (int pass = 0; pass < 2; ++pass) {
     for (int step = 0; step < nblk; ++step) {
-      const int t = pass * nblk + step;
-      // the next step's block streams in while this one is solved (its
-      // buffer was last read before the barrier that ended step t - 1)
-      if (use_pre && t + 1 < 2 * nblk) prefetch(t + 1);
       const int b = pass == 0 ? step : nblk - 1 - step;
       const int k0 = b * 32, nb = min(32, n - k0);
       const int c0 = pass == 0 ? 0 : k0 + nb, c1 = pass == 0 ? k0 : n;
@@ -668,25 +627,7 @@ __device__ void block_lusolve(const T* __restrict__ A, int n, const int* __restr
       }
       T s[4] = {(T)0, (T)0, (T)0, (T)0};
       const int r0 = warp * 4;
-      if (use_pre) {
-        const T* blk = pre + (size_t)(t & 1) * 32 * n;
-        const int L = c1 - c0;
-        for (int j = lane * W; j < L; j += 32 * W) {
-          const V xv = *reinterpret_cast<const V*>(tmp + c0 + j);
-          const T* xe = reinterpret_cast<const T*>(&xv);
-          V av[4];
-#pragma unroll
-          for (int a = 0; a < 4; ++a)
-            if (r0 + a < nb) av[a] = *reinterpret_cast<const V*>(blk + (size_t)(r0 + a) * L + j);
-#pragma unroll
-          for (int a = 0; a < 4; ++a)
-            if (r0 + a < nb) {
-              const T* e = reinterpret_cast<const T*>(&av[a]);
-#pragma unroll
-              for (int w = 0; w < W; ++w) s[a] += e[w] * xe[w];
-            }
-        }
-      } else if (vec) {
+      if (vec) {
         // c0, c1 are multiples of W here (block edges, n % W == 0)
         for (int j = c0 + lane * W; j < c1; j += 32 * W) {
           const V xv = *reinterpret_cast<const V*>(tmp + j);
@@ -740,7 +681,6 @@ __device__ void block_lusolve(const T* __restrict__ A, int n, const int* __restr
         }
         if (lane < nb) tmp[k0 + lane] = v;
       }
-      if (use_pre) cp_async_wait_all();
       __syncthreads();
     }
   }
