@@ -123,16 +123,19 @@ __device__ __forceinline__ void rhs(Ctx<T>& C, const double* y, double* out, boo
 // ---------------------------------------------------------------------------
 // Conservative projection of the mixed path's Newton corrections.  Every
 // reaction conserves the network's invariants c (element counts), so c.f = 0
-// and c.J = 0, hence c.P = c for P = I - h*rl1*J and the exact Newton
-// correction keeps c.acor = 0: each step conserves the invariants to FP64
-// rounding, as the reference's FP64 solve does.  The FP32 factors satisfy
-// c.(P~^-1 r) = c.r only to the FP32 solve's error, amplified by cond(P~),
-// and over ~10^6 steps the residue adds up (1e-5 relative drift measured).
-// At convergence the mixed path therefore removes the invariant component:
-//   acor <- acor - Q C (C^T Q C)^-1 C^T acor,   Q = diag(1/ewt^2),
-// the smallest change of acor in DVODE's weighted norm with C^T acor = 0.
-// G = C^T Q C is formed and inverted at each Jacobian evaluation (with the
-// error weights of that moment), so a step pays two short reductions.
+// and c.J = 0, hence c.P = c for P = I - h*rl1*J: each exact Newton
+// correction leaves c.r, r = rl1*(h*f(y) - zn1) - acor, unchanged, and the
+// converged corrector has c.acor = -rl1 c.zn1 (zn1 the predicted first
+// Nordsieck column), so the invariants hold to FP64 rounding, as in the
+// reference's FP64 solve.  The FP32 factors keep c.(P~^-1 r) = c.r only to
+// the FP32 solve's error, amplified by cond(P~), and over ~10^6 steps the
+// residue adds up (1e-5 relative drift measured on random mass-action
+// networks).  At convergence the mixed path therefore removes it:
+//   acor <- acor - Q C^T G^-1 g,  g = C (acor + rl1 zn1),  G = C Q C^T,
+// Q = diag(1/ewt^2): the smallest change of acor in DVODE's weighted norm
+// that gives the exact corrector's invariant component.  G is formed and
+// inverted at each Jacobian evaluation (with the error weights of that
+// moment), so a step pays two short reductions.
 
 // G and its inverse (Jacobi-scaled Gauss-Jordan, SPD: no pivoting) into
 // W.ginv; an invariant whose scaled pivot vanishes voids the projection
@@ -213,17 +216,27 @@ __device__ void inv_prepare(Ctx<T>& C) {
   __syncthreads();
 }
 
-// acor <- acor - Q C G^-1 C^T acor and y = yh + acor.  All threads call.
+// acor <- acor - Q C^T G^-1 g and y = yh + acor, g = C (acor + rl1 zn1).
+// The exact corrector solution has acor = rl1 (h f(y) - zn1) with zn1 the
+// predicted first Nordsieck column, so C acor = -rl1 C zn1 (C f = 0); the
+// residue g is the part of the Newton iterate's error that breaks the
+// invariants.  (Projecting to C acor = 0 instead would keep any invariant
+// part of zn1 out of reach of the corrector, which restores zn1 = h f(y)
+// after each step; that part then grows through the predictor.)  All
+// threads call.
 template <typename T>
 __device__ void inv_project(Ctx<T>& C) {
   const DevNet& N = *C.N;
   Shared& sh = *C.sh;
   const int E = N.n_inv, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, n = C.n;
+  const double* zn1 = C.W.yh + n;
+  const double rl1 = sh.d.rl1;
   for (int e = warp; e < E; e += NWARP) {
     double s = 0.0;
     for (int k = N.inv_el_ptr[e] + lane; k < N.inv_el_ptr[e + 1]; k += 32) {
       const unsigned w = N.inv_el[k];
-      s += coef_to_double((signed char)(w & 0xFFu)) * C.acor[w >> 8];
+      const int i = (int)(w >> 8);
+      s += coef_to_double((signed char)(w & 0xFFu)) * (C.acor[i] + rl1 * zn1[i]);
     }
     s = warp_sum(s);
     if (lane == 0) sh.inv_g[e] = s;
