@@ -404,7 +404,7 @@ def our_arm(args):
         pass
     peak = float(peaks.get("bf16_tflops", FALLBACK_BF16_TFLOPS))
     peak_src = "measured" if "bf16_tflops" in peaks else "fallback"
-    cpu = cpu_estimate(dicts, args.cpu_sample, os.cpu_count() or 1) if world == 1 else None
+    cpu = cpu_estimate(dicts, args.cpu_sample, os.cpu_count() or 1) if world == 1 and args.cpu_sample > 0 else None
     nslots = ctx.slots(_lib.PREC_MIXED)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,

@@ -8,13 +8,14 @@ reference's rates + GETYDOT + DVODE MF=22 path) on a seeded sample of the
   (int16 milli-dex, clamped at -16 dex: only species above 1e-14 are
   compared), and the oracle's CPU time; plus, for every 8th model of the
   sample, the same model at reltol 1e-12 (mxstep 100000) as the "truth" for
-  the mixed-precision error statement.
+  the mixed-precision error statement.  `--add-truth I [I ...]` appends
+  truth runs for more sample points (the parity outliers) to the file.
 
 The runs take the oracle tens of CPU-minutes per slow model; they run in a
 process pool, each capped in CPU time (2400 s at the reference's tolerance,
 1200 s for a truth run): a capped run is stored with the oracle's cap flag
 (-99) and no rows, and the tests skip it.
-Usage: python tests/golden/make_grid_sample.py [--procs N]
+Usage: python tests/golden/make_grid_sample.py [--procs N] [--add-truth I ...]
 """
 import argparse
 import multiprocessing as mp
@@ -61,12 +62,41 @@ def run(task):
     return i, tight, int(flag), len(phys), cnt, phys[:, 0].copy(), quantize(ab), time.process_time() - t
 
 
+def _pack(res, order):
+    """Fixture arrays of a list of run() results, in the order of `order`."""
+    rr = sorted(res, key=lambda r: order.index(r[0]))
+    m = len(rr)
+    q = np.full((m, ROWS, 335), FLOOR_MDEX, dtype=np.int16)
+    tyr = np.zeros((m, ROWS))
+    for k, r in enumerate(rr):
+        q[k, : r[3]] = r[6]
+        tyr[k, : r[3]] = r[5]
+    return {"index": np.array([r[0] for r in rr], dtype=np.int32),
+            "flag": np.array([r[2] for r in rr], dtype=np.int32),
+            "nrows": np.array([r[3] for r in rr], dtype=np.int32),
+            "counters": np.array([r[4] for r in rr], dtype=np.int64),
+            "tyears": tyr, "log10_mdex": q, "cpu_s": np.array([r[7] for r in rr])}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--procs", type=int, default=os.cpu_count() or 1)
+    ap.add_argument("--add-truth", type=int, nargs="+", default=None)
     args = ap.parse_args()
     from uclchem_gb300.params import grid_params, stratified_sample
     dicts = grid_params(4096, seed=SEED, final_time=1e6)
+    path = os.path.join(HERE, "grid_sample_1e6yr.npz")
+    if args.add_truth:
+        old = dict(np.load(path))
+        extra = [i for i in args.add_truth if i in set(old["index"].tolist()) and i not in set(old["tight_index"].tolist())]
+        with mp.get_context("spawn").Pool(min(args.procs, max(1, len(extra)))) as pool:
+            res = pool.map(run, [(i, dicts[i], True) for i in extra], chunksize=1)
+        new = _pack(res, extra)
+        for k, v in new.items():
+            old["tight_" + k] = np.concatenate([old["tight_" + k], v])
+        np.savez_compressed(path, **old)
+        print("appended truth runs", extra, "flags", new["flag"], "cpu_s", new["cpu_s"].round())
+        return
     idx = stratified_sample(dicts, SAMPLE, seed=SEED + 3)
     tight = idx[::8]
     tasks = [(i, dicts[i], False) for i in idx] + [(i, dicts[i], True) for i in tight]
@@ -75,23 +105,11 @@ def main():
     with mp.get_context("spawn").Pool(args.procs) as pool:
         res = pool.map(run, tasks, chunksize=1)
     out = {}
-    for tag, sel in (("", False), ("tight_", True)):
-        rr = sorted([r for r in res if r[1] == sel], key=lambda r: (idx if not sel else tight).index(r[0]))
-        m = len(rr)
-        q = np.full((m, ROWS, 335), FLOOR_MDEX, dtype=np.int16)
-        tyr = np.zeros((m, ROWS))
-        for k, r in enumerate(rr):
-            q[k, : r[3]] = r[6]
-            tyr[k, : r[3]] = r[5]
-        out[tag + "index"] = np.array([r[0] for r in rr], dtype=np.int32)
-        out[tag + "flag"] = np.array([r[2] for r in rr], dtype=np.int32)
-        out[tag + "nrows"] = np.array([r[3] for r in rr], dtype=np.int32)
-        out[tag + "counters"] = np.array([r[4] for r in rr], dtype=np.int64)
-        out[tag + "tyears"] = tyr
-        out[tag + "log10_mdex"] = q
-        out[tag + "cpu_s"] = np.array([r[7] for r in rr])
-    np.savez_compressed(os.path.join(HERE, "grid_sample_1e6yr.npz"), seed=SEED, **out)
-    print("wrote", os.path.join(HERE, "grid_sample_1e6yr.npz"))
+    for tag, sel, order in (("", False, idx), ("tight_", True, tight)):
+        for k, v in _pack([r for r in res if r[1] == sel], order).items():
+            out[tag + k] = v
+    np.savez_compressed(path, seed=SEED, **out)
+    print("wrote", path)
     for k in range(len(out["index"])):
         print(out["index"][k], "%.3g" % dicts[out["index"][k]]["initialDens"], out["flag"][k], out["nrows"][k],
               out["counters"][k][:4], "%.1f s" % out["cpu_s"][k])

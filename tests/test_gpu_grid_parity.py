@@ -21,9 +21,19 @@ pytestmark = pytest.mark.gpu
 FIX = os.path.join(GOLDEN, "grid_sample_1e6yr.npz")
 ROWS = 501
 # Grid points whose result at the reference's tolerance is set by the
-# integration path rather than by the arithmetic: index -> reason.  They
-# must still end with the oracle's flag; their dex bound is not applied.
-OUTLIERS = {}
+# integration path rather than by the arithmetic: index -> reason.  Each
+# has a reltol-1e-12 oracle run in the fixture; the device must end with the
+# oracle's flag and be at least as close to that truth as the oracle at the
+# reference's tolerance is (test_outliers_are_no_further_from_the_truth).
+OUTLIERS = {3767: "late-time S2 and N-ice chemistry (n = 4.7e4, T = 39 K, G = 582): the reltol-1e-8 oracle is "
+                  "0.44 dex from its reltol-1e-10 run at 1e6 yr; the device 0.09 (FP64) / 0.02 (mixed)"}
+# Grid points where the oracle ends with -5 (integration failure after the
+# retries of updateChemistry) and the device completes: in each, the
+# oracle's Newton iteration with DVODE's finite-difference Jacobian fails on
+# more than 5% of its steps, the device's with the analytic Jacobian on
+# under 1% (checked below).
+FD_JACOBIAN_FAILURES = {1558: "oracle: 23145 Newton failures in 319958 steps",
+                        2535: "oracle: 29615 Newton failures in 275244 steps"}
 CAPPED = -99  # the oracle's run hit its CPU-time cap when the fixture was made: no reference result
 
 
@@ -107,7 +117,13 @@ def test_grid_sample_matches_oracle(runs, precision):
         if fx["flag"][k] == CAPPED:
             continue
         if fl[k] != fx["flag"][k]:
+            cnt = fx["counters"][k]
+            if (int(i) in FD_JACOBIAN_FAILURES and fx["flag"][k] == -5 and fl[k] == 0
+                    and cnt[5] > 0.05 * cnt[0] and st["ncfn"][k] < 0.01 * st["nst"][k]):
+                continue
             flags.append((int(i), int(fl[k]), int(fx["flag"][k])))
+            continue
+        if fl[k] != 0:
             continue
         oab, otyr = _oracle_rows(fx, k)
         r = int(nr[k])
@@ -128,15 +144,26 @@ def test_grid_sample_matches_oracle(runs, precision):
 
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
 def test_grid_sample_step_counts_follow_the_oracle(runs, precision):
-    """The device takes DVODE's decisions; with the analytic Jacobian (and the
-    FP32 factorisation on the mixed path) the step counts stay within a
-    band of the oracle's finite-difference-Jacobian counts."""
+    """The device takes DVODE's decisions, so its step counts follow the
+    oracle's: median ratio 0.95-1.1, none above 2x.  The exception is where
+    the oracle's Newton iteration with DVODE's finite-difference Jacobian
+    keeps failing (Newton plus error-test failures on 5% of its steps or
+    more, each failure shrinking the step): there the analytic Jacobian,
+    whose Newton iteration fails on under 1% of the device's steps, needs
+    fewer steps, down to a few percent of the oracle's."""
     fx, out = runs
     st, fl = out[precision][4], out[precision][3]
-    ok = (fl == 0) & (fx["flag"] == 0)
-    ratio = st["nst"][ok] / fx["counters"][ok, 0]
+    ok = np.nonzero((fl == 0) & (fx["flag"] == 0))[0]
+    cnt = fx["counters"][ok]
+    ratio = st["nst"][ok] / cnt[:, 0]
     assert 0.95 <= np.median(ratio) <= 1.1, np.median(ratio)
-    assert ratio.min() > 0.5 and ratio.max() < 2.0, (ratio.min(), ratio.max())
+    assert ratio.max() < 2.0, [(int(fx["index"][k]), r) for k, r in zip(ok, ratio) if r >= 2.0]
+    low = ratio < 0.5
+    fd_fail = (cnt[:, 5] + cnt[:, 6]) >= 0.05 * cnt[:, 0]
+    dev_ok = st["ncfn"][ok] < 0.01 * st["nst"][ok]
+    odd = low & ~(fd_fail & dev_ok)
+    assert not odd.any(), [(int(fx["index"][k]), round(float(r), 3), [int(x) for x in c[:7]])
+                           for k, r, c in zip(ok[odd], ratio[odd], cnt[odd])]
 
 
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
@@ -153,22 +180,48 @@ def test_grid_sample_conserves_elements(runs, net, precision):
     assert worst < 1e-10, worst
 
 
+def _truth_errors(fx, out, precision, k, j, sched):
+    """(device, oracle) max |dex| against the truth run j of sample point k,
+    at the schedule times all three reached."""
+    ph, ab, nr, fl, st = out[precision]
+    truth, ttyr = _oracle_rows(fx, j, "tight_")
+    ref, rtyr = _oracle_rows(fx, k)
+    t_at, r_at = _rows_at(ttyr, sched), _rows_at(rtyr, sched)
+    g_at = _rows_at(ph[k, : nr[k], 0], sched)
+    m = (t_at >= 0) & (r_at >= 0) & (g_at >= 0)
+    return dex_error(ab[k, g_at[m]], truth[t_at[m]]), dex_error(ref[r_at[m]], truth[t_at[m]])
+
+
 def test_mixed_error_against_tight_tolerance_truth(runs):
     """Configuration 3's error statement: on every 8th sample point, the
     mixed path's max |dex| against the oracle at reltol 1e-12 is at most the
     reference-tolerance oracle's own |dex| against it plus 0.01."""
     fx, out = runs
-    ph, ab, nr, fl, st = out[1]
+    fl = out[1][3]
+    sched = _schedule(fx)
     pos = {int(i): k for k, i in enumerate(fx["index"])}
+    checked = 0
     for j, i in enumerate(fx["tight_index"]):
         k = pos[int(i)]
-        if fx["tight_flag"][j] != 0 or fl[k] != 0 or fx["flag"][k] != 0:
+        if int(i) in OUTLIERS or fx["tight_flag"][j] != 0 or fl[k] != 0 or fx["flag"][k] != 0:
             continue
-        truth, ttyr = _oracle_rows(fx, j, "tight_")
-        ref, rtyr = _oracle_rows(fx, k)
-        r = min(len(ttyr), int(nr[k]), len(rtyr))
-        if not (np.allclose(ttyr[:r], ph[k, :r, 0], rtol=1e-12) and np.allclose(rtyr[:r], ttyr[:r], rtol=1e-12)):
-            continue  # retries changed the output times: rows are not comparable
-        e_mixed = dex_error(ab[k, :r], truth[:r])
-        e_ref = dex_error(ref[:r], truth[:r])
+        e_mixed, e_ref = _truth_errors(fx, out, 1, k, j, sched)
         assert e_mixed <= e_ref + 0.01, (int(i), e_mixed, e_ref)
+        checked += 1
+    assert checked >= 5, checked
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_outliers_are_no_further_from_the_truth(runs, precision):
+    """Every parity outlier: the device's max |dex| against the oracle's
+    reltol-1e-12 run is at most the reltol-1e-8 oracle's own plus 0.01."""
+    fx, out = runs
+    fl = out[precision][3]
+    sched = _schedule(fx)
+    pos = {int(i): k for k, i in enumerate(fx["index"])}
+    tpos = {int(i): j for j, i in enumerate(fx["tight_index"])}
+    for i in OUTLIERS:
+        k, j = pos[i], tpos[i]
+        assert fx["tight_flag"][j] == 0 and fl[k] == fx["flag"][k] == 0, (i, int(fl[k]))
+        e_dev, e_ref = _truth_errors(fx, out, precision, k, j, sched)
+        assert e_dev <= e_ref + 0.01, (i, e_dev, e_ref)

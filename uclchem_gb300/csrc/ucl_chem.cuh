@@ -436,7 +436,7 @@ __device__ __forceinline__ double flux_of(int sh, double k, double D, double ya,
 //   warp 0: CO photodissociation (lane-parallel shielding splines)
 //   warp 1: H2 photodissociation
 //   warps 2..: the other reaction fluxes
-__device__ void dev_rhs(const DevNet& N, const ucl_model_params& P, const SysPhys& S, const double* y,
+__device__ __noinline__ void dev_rhs(const DevNet& N, const ucl_model_params& P, const SysPhys& S, const double* y,
                         const double* rate, double* ydot, double* flux, double* part, RhsScal& R,
                         bool jac_scalars = false) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -612,7 +612,7 @@ __device__ void dev_rhs(const DevNet& N, const ucl_model_params& P, const SysPhy
 // Otherwise J stored as double.  Must follow a dev_rhs(..., jac_scalars=true)
 // on the same y (uses R, flux).  dfa/dfb: [nreac] shared scratch.
 template <bool SCALED, typename T>
-__device__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhys& S, const double* y,
+__device__ __noinline__ void dev_jac(const DevNet& N, const ucl_model_params& P, const SysPhys& S, const double* y,
                         const double* rate, const double* w, const double* wi, T* J, const double* flux,
                         double* dfa, double* dfb, double* vec, double* jpart, const RhsScal& R) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
