@@ -48,9 +48,9 @@ SEED = 20261203
 ROWS = 501          # TIMEPOINTS + 1 (src/uclchem/constants.py:22)
 # DRAM bytes (read + write) of the mixed solver per model-step, from one ncu
 # capture (dram__bytes_read.sum + dram__bytes_write.sum) of the 152-model,
-# 1e4-yr grid launch: 113.6 GB over 152 x 4094 model-steps.  Traffic scales
+# 1e4-yr grid launch: 161.2 GB over 152 x 4187.6 model-steps.  Traffic scales
 # with model-steps once the slots' working set exceeds L2.
-DRAM_BYTES_PER_MODEL_STEP = 1.83e5
+DRAM_BYTES_PER_MODEL_STEP = 2.53e5
 FALLBACK_BF16_TFLOPS = 1900.0
 
 
