@@ -13,8 +13,8 @@ reference's rates + GETYDOT + DVODE MF=22 path) on a seeded sample of the
 
 The runs take the oracle tens of CPU-minutes per slow model; they run in a
 process pool, each capped in CPU time (2400 s at the reference's tolerance,
-1200 s for a truth run): a capped run is stored with the oracle's cap flag
-(-99) and no rows, and the tests skip it.
+1200 s for a truth run, 3600 s for an appended one): a capped run is stored
+with the oracle's cap flag (-99) and no rows, and the tests skip it.
 Usage: python tests/golden/make_grid_sample.py [--procs N] [--add-truth I ...]
 """
 import argparse
@@ -32,6 +32,7 @@ sys.path.insert(0, ROOT)
 SEED = 20261203
 SAMPLE = 64
 CAP_S = {False: 2400.0, True: 1200.0}
+ADD_TRUTH_CAP_S = 3600.0
 ROWS = 501
 FLOOR_MDEX = -16000
 
@@ -47,7 +48,8 @@ _ORC = None
 
 def run(task):
     global _ORC
-    i, d, tight = task
+    i, d, tight = task[:3]
+    cap = task[3] if len(task) > 3 else CAP_S[tight]
     if _ORC is None:
         from oracle.oracle import Oracle
         _ORC = Oracle()
@@ -56,7 +58,7 @@ def run(task):
     if tight:
         p["reltol"] = 1e-12
         p["mxstep"] = 100000
-    _ORC.set_cpu_limit(CAP_S[tight])
+    _ORC.set_cpu_limit(cap)
     t = time.process_time()
     phys, ab, flag, cnt = _ORC.cloud(p, max_rows=ROWS)
     return i, tight, int(flag), len(phys), cnt, phys[:, 0].copy(), quantize(ab), time.process_time() - t
@@ -90,7 +92,7 @@ def main():
         old = dict(np.load(path))
         extra = [i for i in args.add_truth if i in set(old["index"].tolist()) and i not in set(old["tight_index"].tolist())]
         with mp.get_context("spawn").Pool(min(args.procs, max(1, len(extra)))) as pool:
-            res = pool.map(run, [(i, dicts[i], True) for i in extra], chunksize=1)
+            res = pool.map(run, [(i, dicts[i], True, ADD_TRUTH_CAP_S) for i in extra], chunksize=1)
         new = _pack(res, extra)
         for k, v in new.items():
             old["tight_" + k] = np.concatenate([old["tight_" + k], v])

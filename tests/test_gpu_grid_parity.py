@@ -25,8 +25,9 @@ ROWS = 501
 # has a reltol-1e-12 oracle run in the fixture; the device must end with the
 # oracle's flag and be at least as close to that truth as the oracle at the
 # reference's tolerance is (test_outliers_are_no_further_from_the_truth).
-OUTLIERS = {3767: "late-time S2 and N-ice chemistry (n = 4.7e4, T = 39 K, G = 582): the reltol-1e-8 oracle is "
-                  "0.44 dex from its reltol-1e-10 run at 1e6 yr; the device 0.09 (FP64) / 0.02 (mixed)"}
+OUTLIERS = {3767: "late-time S2 and N-ice chemistry (n = 4.7e4, T = 39 K, G = 582) that no tolerance "
+                  "settles: at 1e6 yr the oracle at reltol 1e-8 is 0.69 dex from its reltol-1e-12 run, and its "
+                  "reltol-1e-10 run 0.29 dex; the device is 0.34 (FP64) / 0.30 (mixed) dex from it"}
 # Grid points where the oracle ends with -5 (integration failure after the
 # retries of updateChemistry) and the device completes: in each, the
 # oracle's Newton iteration with DVODE's finite-difference Jacobian fails on

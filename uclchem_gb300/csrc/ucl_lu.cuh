@@ -311,9 +311,10 @@ __device__ __forceinline__ int panel_factor(T* __restrict__ A, int n, int k0, in
 // scratch for the row interchanges outside the panel; perm: shared [n].
 // tc: tensor-core state of the CTA (TMEM + mbarrier) or nullptr for the
 // CUDA-core trailing update.
-// Not inlined (nor block_lusolve, dev_rhs, dev_jac): inside the 255-register
-// solver kernel each then gets a register allocation of its own; measured on
-// 152 grid models, 272 -> 267 us per BDF step, the factorisation 637 -> 517 us.
+// Not inlined (nor dev_rhs, dev_jac): inside the 255-register solver kernel
+// each then gets a register allocation of its own; measured on 152 grid
+// models, 272 -> 265 us per BDF step, the factorisation 637 -> 516 us (the
+// triangular solve is faster inlined).
 template <typename T>
 __device__ __noinline__ int block_lu(T* __restrict__ A, int n, int* __restrict__ perm_out, char* smem, int* s_i,
                          T* __restrict__ scr, int* perm, TcState* tc = nullptr) {
@@ -599,7 +600,7 @@ __device__ void lu_diag_inverses(const T* __restrict__ A, int n, T* __restrict__
 // the system solved is (LU) x = W y and y <- W^-1 x, with W = diag(ws) and
 // W^-1 = diag(wis) (both nullptr: no scaling).
 template <typename T>
-__device__ __noinline__ void block_lusolve(const T* __restrict__ A, int n, const int* __restrict__ perm,
+__device__ void block_lusolve(const T* __restrict__ A, int n, const int* __restrict__ perm,
                               const T* __restrict__ dinv, double* y, const double* ws, const double* wis, T* tmp,
                               T* rbuf) {
   using V = typename Vec2<T>::type;
