@@ -578,7 +578,10 @@ def serve_arm(args):
                       "p50_solve_ms": float(np.percentile(solve_ms, 50)),
                       "p99_solve_ms": float(np.percentile(solve_ms, 99)),
                       "latency": "host-observed: Poisson arrival time to the poll that sees the request done",
-                      "failed": int((flags != 0).sum()), "slots": ctx.slots(_lib.PREC_MIXED)}), flush=True)
+                      "failed": int((flags != 0).sum()),
+                      "failed_codes": {str(int(c)): int((flags == c).sum()) for c in np.unique(flags[flags != 0])},
+                      "arrivals_s": float(arrival[-1]),
+                      "slots": ctx.slots(_lib.PREC_MIXED)}), flush=True)
     ctx.close()
 
 
