@@ -70,6 +70,12 @@ typedef struct ucl_model_params {
   int32_t enforceChargeConservation, improvedH2CRPDissociation;
   int32_t cosmicRayAttenuation; /* column-density CR attenuation, physics-core.f90:121-157 */
   int32_t ionModel;             /* 'L' or 'H' (character code), defaultparameters.f90:47 */
+  /* physics module: 0 = the static/freefall CLOUD of cloud.f90; 1-4 = the
+   * parameterised prestellar-core collapse of collapse.f90 (Priestley et al.
+   * 2018): 1 'BE1.1', 2 'BE4', 3 'filament', 4 'ambipolar', the collapse
+   * argument of uclchem.model.collapse (model.py:355, wrap.f90:83-152) */
+  int32_t collapse;
+  int32_t reserved; /* 0 */
 } ucl_model_params;
 
 /* Fill *p with the reference defaults (defaultparameters.f90:18-119). */
@@ -187,8 +193,12 @@ typedef struct ucl_model_stats {
  * Per-model options the reference rejects at start-up give that model
  * UCL_PHYSICS_INIT_ERROR and no rows: ionModel other than 'L'/'H',
  * improvedH2CRPDissociation without cosmicRayAttenuation
- * (physics-core.f90:55-64), and points != 1 (the reference's multi-parcel
- * column density reads coldens(0), outside its array, physics-core.f90:80). */
+ * (physics-core.f90:55-64), a collapse mode other than 0-4
+ * (collapse.f90:44-48), and points != 1 (the reference's multi-parcel
+ * column density reads coldens(0), outside its array, physics-core.f90:80).
+ * With collapse 1-4 the model runs collapse.f90's physics module: its
+ * initializePhysics (BE1.1 and BE4 set finalTime to 0.97 of their maxTime),
+ * updateTargetTime and updatePhysics between intervals. */
 int ucl_solve_models(ucl_ctx* ctx, int nmodels, const ucl_model_params* params,
                      const double* start, int max_rows, double* phys_out,
                      double* abund_out, int* nrows_out, int* flag_out,

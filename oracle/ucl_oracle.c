@@ -1737,6 +1737,159 @@ static void write_row(const chem_t* c, const model_t* m, double* phys, double* a
   }
 }
 
+/* ---------------------------------------------------------------------- */
+/* The collapse physics module (collapse.f90, Priestley et al. 2018): modes
+ * 1 BE1.1, 2 BE4, 3 filament, 4 ambipolar.  Default-REAL literals are
+ * single precision promoted (SP), 'd' literals double; integer powers by
+ * the binary method (ipow_bin).  The sums run left to right, as the
+ * reference's loops do. */
+static const double COL_MH = 1.67262164e-24, COL_AU = 2.063e5; /* constants.f90:7,12 */
+
+static double col_unitr(void) { /* collapse.f90:190-191 */
+  return sqrt(1.38e-16 * 10 / 2 / COL_MH) * pow(2 * PI_ * 6.67e-8 * 2.2e4 * COL_MH, -0.5) / PC;
+}
+static double col_unitt(void) { /* collapse.f90:209-210 */
+  return pow(2 * PI_ * 6.67e-8 * 2.2e4 * COL_MH, -0.5) / SECONDS_PER_YEAR;
+}
+
+static double rhofit(int mode, double r, double rho0, double r0, double a) { /* collapse.f90:178-196 */
+  if (mode == 1 || mode == 2) return rho0 / (1 + pow(r * COL_AU / r0, a));
+  if (mode == 3) {
+    double x = r / col_unitr() / r0;
+    return 2.2e4 * rho0 / pow(1 + x * x, a);
+  }
+  return rho0 / (1 + pow(r / 7.5e-1 / r0, a));
+}
+
+static double rho0fit(int mode, double t, double tmax) { /* collapse.f90:199-222 */
+  double l;
+  if (mode == 1) l = SP(61.8) * pow(tmax - t, SP(-0.01)) - SP(49.4);
+  else if (mode == 2) l = SP(68.4) * pow(tmax - t, SP(-0.01)) - SP(55.7);
+  else if (mode == 3) l = SP(3.54) * pow(SP(5.47) - t / col_unitt(), SP(-0.15)) - SP(2.73);
+  else {
+    if (t <= 6.0) return 2.0e3 + 1.7e3 * (t / 6.0 - 1.0);
+    l = SP(5.3) * pow(SP(16.138) - 1e-6 * t, SP(-0.1)) - 1.0;
+  }
+  return pow(10.0, l);
+}
+
+static double r0fit(int mode, double t, double tmax) { /* collapse.f90:225-245 */
+  double l;
+  if (mode == 1) l = -(SP(28.5) * pow(tmax - t, SP(-0.01))) + SP(28.93);
+  else if (mode == 2) l = -(SP(39.0) * pow(tmax - t, SP(-0.01))) + SP(38.7);
+  else if (mode == 3) l = -(SP(1.34) * pow(SP(5.47) - t / col_unitt(), SP(-0.15))) + SP(1.47);
+  else l = -(SP(2.57) * pow(SP(16.138) - 1e-6 * t, SP(-0.1))) + SP(1.85);
+  return pow(10.0, l);
+}
+
+static double afit(int mode, double t) { /* collapse.f90:248-261 */
+  if (mode == 1) return 2.4;
+  if (mode == 2) return SP(1.9) + 0.5 * exp(-t / SP(1e5));
+  if (mode == 3) return 2.0 - 0.5 * ipow_bin(t / col_unitt() / SP(5.47), 9);
+  return SP(2.4) - SP(0.2) * ipow_bin(1e-6 * t / SP(16.138), 40);
+}
+
+static double vrfit(int mode, double r, double rmin, double vmin, double a) { /* collapse.f90:264-290 */
+  double v;
+  if (mode == 3) {
+    double nr = r / col_unitr() - rmin;
+    if (nr < 0.0) v = vmin * ((nr / rmin) * (nr / rmin) - 1);
+    else v = vmin * (exp(-2.0 * a * nr) - 2 * exp(-a * nr));
+    return sqrt(1.38e-16 * 10 / 2 / COL_MH) * v;
+  }
+  if (mode == 4) {
+    double rmid = 0.5, r75 = r / 7.5e-1, nr = r75 - rmin;
+    if (r75 < rmin) v = vmin * ((nr / rmin) * (nr / rmin) - 1);
+    else if (r75 <= rmid) v = (vmin - a) * pow(nr / (rmid - rmin), SP(0.3)) - vmin;
+    else v = a / (1.0 - rmid) * (r75 - rmid) - a;
+    return 1e3 * v;
+  }
+  return 0.0;
+}
+
+static double rminfit(int mode, double t) { /* collapse.f90:293-321 */
+  if (mode == 3) {
+    double tn = t / col_unitt();
+    if (tn == 0.0) return 7.2;
+    if (log(tn) < 1.6) return -(SP(1.149) * tn) + SP(7.2);
+    if (log(tn) < 1.674) return -(SP(9.2) * log(tn)) + SP(16.25);
+    return -(SP(22.0) * log(tn)) + SP(37.65);
+  }
+  double t6 = 1e-6 * t;
+  if (t6 <= SP(10.2)) return -(SP(0.0039) * t6) + SP(0.49);
+  if (t6 <= SP(15.1)) return -(SP(0.0306) * (t6 - SP(10.2))) + SP(0.45);
+  return -(SP(0.282) * (t6 - SP(15.1))) + SP(0.3);
+}
+
+static double vminfit(int mode, double t) { /* collapse.f90:324-346 */
+  if (mode == 3) {
+    double tn = t / col_unitt();
+    if (tn == 0.0) return 0.0;
+    if (log(tn) < 1.6) return SP(0.0891) * tn;
+    if (log(tn) < 1.674) return SP(5.5) * log(tn) - SP(8.37);
+    return SP(18.9) * log(tn) - SP(30.8);
+  }
+  return SP(3.44) * pow(SP(16.138) - 1e-6 * t, SP(-0.35)) - SP(0.7);
+}
+
+static double avfit(int mode, double t) { /* collapse.f90:349-378 */
+  if (mode == 3) {
+    double tn = t / col_unitt();
+    if (tn == 0.0) return 0.4;
+    if (log(tn) < 1.6) return SP(0.0101) * tn + SP(0.4);
+    if (log(tn) < 1.674) return SP(0.695) * log(tn) - SP(0.663);
+    return SP(2.69) * log(tn) - SP(4.0);
+  }
+  double t6 = 1e-6 * t;
+  if (t6 <= SP(10.2)) return SP(0.143) * t6;
+  return SP(0.217) * (t6 - SP(10.2)) + SP(1.46);
+}
+
+static double find_coldens(int mode, double rin, double rho0, double r0, double a, double rout) {
+  /* collapse.f90:157-175 */
+  const int np = 10000;
+  double size = rout - rin, dr = size / np, coldens = 0.0;
+  if (size <= 0.0) return coldens;
+  for (int i = 1; i <= np; i++) {
+    double r1 = rin + (i - 1) * dr, r2 = rin + i * dr;
+    double drho = 0.5 * (rhofit(mode, r2, rho0, r0, a) + rhofit(mode, r1, rho0, r0, a));
+    coldens = coldens + drho * dr * PC;
+  }
+  return coldens;
+}
+
+static double find_mass_in_radius(int mode, double radius, double rho0, double r0, double a) {
+  /* collapse.f90:117-134 */
+  const int np = 1000;
+  double dr = radius / np, m = 0.0;
+  for (int i = 1; i <= np; i++) {
+    double drho = 0.5 * (rhofit(mode, i * dr, rho0, r0, a) + rhofit(mode, (i - 1) * dr, rho0, r0, a));
+    m = m + drho * dr * ((i * dr) * (i * dr));
+  }
+  return m;
+}
+
+static double find_new_radius(int mode, double mass, double r, double rho0, double r0, double a) {
+  /* collapse.f90:137-154; -1 if the mass is not positive or not reached in
+   * 2^24 steps (the reference would return an unset value or loop on) */
+  double dr = r / 1.0e4, m1 = 0.0, rad = -1.0;
+  if (!(0.0 < mass)) return -1.0;
+  for (int i = 1; i < (1 << 24) + 1; i++) {
+    double drho = 0.5 * (rhofit(mode, i * dr, rho0, r0, a) + rhofit(mode, (i - 1) * dr, rho0, r0, a));
+    m1 = m1 + drho * dr * ((i * dr) * (i * dr));
+    rad = i * dr;
+    if (!(m1 < mass)) return rad;
+  }
+  return -1.0;
+}
+
+static double col_target_time(double ty) { /* collapse.f90:60-72 */
+  if (ty > 10000) return (ty + 1000.0) * SECONDS_PER_YEAR;
+  if (ty > 1000) return (ty + 100.0) * SECONDS_PER_YEAR;
+  if (ty > 0.0) return (ty * 10) * SECONDS_PER_YEAR;
+  return 3.16e7 * 10.e-8;
+}
+
 /* A whole CLOUD model (solveAbundances, wrap.f90:549-697, points=1), with
  * the rows of the rates array when rates_rows is not NULL */
 int orc_cloud_rates(const orc_net* n, const ucl_model_params* p, const double* start, int max_rows, double* phys,
@@ -1754,6 +1907,26 @@ int orc_cloud_rates(const orc_net* n, const ucl_model_params* p, const double* s
     memcpy(m.abund, start, sizeof(double) * (size_t)n->nspec);
     m.abund[neq - 1] = start[n->nspec];
   }
+  /* collapse module: initializePhysics (collapse.f90:27-58) after the
+   * core's, then initializeChemistry's abund(neq) = density */
+  const int cmode = p->collapse;
+  double ctmax = 0.0, crad = 0.0, cmass = 0.0;
+  if (cmode != 0) {
+    if (cmode < 1 || cmode > 4) {
+      chem_free(&c); free(m.abund); free(m.abstol);
+      *nrows = 0;
+      return UCL_PHYSICS_INIT_ERROR; /* "unacceptable collapse mode" */
+    }
+    if (cmode == 1) ctmax = 1.175e6;
+    if (cmode == 2) ctmax = 1.855e5;
+    if (cmode <= 2) c.p.finalTime = SP(0.97) * ctmax;
+    crad = 1 * p->rout / (double)(float)p->points;
+    double rho0 = rho0fit(cmode, 0.0, ctmax), r0 = r0fit(cmode, 0.0, ctmax), a = afit(cmode, 0.0);
+    c.density = rhofit(cmode, p->rin, rho0, r0, a);
+    if (cmode <= 2) cmass = find_mass_in_radius(cmode, crad, rho0, r0, a);
+    if (!start) m.abund[neq - 1] = c.density;
+  }
+  const ucl_model_params* pp = &c.p;
   dv_alloc(&m.dv, neq);
   m.abstol_factor = p->abstol_factor;
   int flag = 0, row = 0;
@@ -1762,11 +1935,12 @@ int orc_cloud_rates(const orc_net* n, const ucl_model_params* p, const double* s
   if (max_rows < 1) flag = UCL_NOT_ENOUGH_TIMEPOINTS_ERROR;
   else write_row(&c, &m, phys, abund_rows, rates_rows, 0);
   row = 1;
-  while (flag == 0 && ((p->endAtFinalDensity && c.density < p->finalDens) ||
-                       (!p->endAtFinalDensity && m.timeInYears < p->finalTime))) {
+  while (flag == 0 && ((pp->endAtFinalDensity && c.density < pp->finalDens) ||
+                       (!pp->endAtFinalDensity && m.timeInYears < pp->finalTime))) {
     double told = m.currentTime;
     m.timeInYears = m.currentTime / SECONDS_PER_YEAR;
-    update_target_time(&m);
+    if (cmode) m.targetTime = col_target_time(m.timeInYears);
+    else update_target_time(&m);
     m.currentTime = told;
     flag = update_chemistry(&m, &c);
     if (flag < 0) break;
@@ -1777,6 +1951,21 @@ int orc_cloud_rates(const orc_net* n, const ucl_model_params* p, const double* s
     c.dustTemp = c.gasTemp;
     if (p->cosmicRayAttenuation && p->improvedH2CRPDissociation) c.h2CRPRate = h2_crp_rate(p, c.coldens);
     if (row >= max_rows) { flag = UCL_NOT_ENOUGH_TIMEPOINTS_ERROR; break; }
+    if (cmode) {
+      /* the collapse module's updatePhysics (collapse.f90:76-106) */
+      double t = m.timeInYears;
+      double rho0 = rho0fit(cmode, t, ctmax), r0 = r0fit(cmode, t, ctmax), a = afit(cmode, t);
+      c.coldens = find_coldens(cmode, p->rin, rho0, r0, a, p->rout);
+      c.av = p->baseAv + c.coldens / 1.6e21;
+      if (cmode <= 2) {
+        crad = find_new_radius(cmode, cmass, p->rout, rho0, r0, a);
+      } else {
+        double dt = m.targetTime - m.currentTime; /* zero: the chemistry reached targetTime */
+        crad = crad + vrfit(cmode, crad, rminfit(cmode, t), vminfit(cmode, t), avfit(cmode, t)) * dt / PC;
+      }
+      if (!(crad >= 0.0)) { flag = UCL_INT_UNRECOVERABLE_ERROR; break; }
+      c.density = rhofit(cmode, crad, rho0, r0, a);
+    }
     write_row(&c, &m, phys + (size_t)row * UCL_N_PHYS, abund_rows + (size_t)row * n->nspec,
               rates_rows ? rates_rows + (size_t)row * n->nreac : NULL, row);
     row++;

@@ -36,6 +36,8 @@ struct DvState {
 
 struct ModelState {
   double t, target, orig, tyears, abstol_factor, dens, coldens;
+  double ctmax, crad, cmass;  // collapse module: maxTime, parcel radius (pc), mass inside it
+  int cmode;                  // 0 cloud, 1-4 collapse modes
   int flag, row, loop, fail_count, retries, model, go;
   long long nst, nfe, nje, nlu, nni, ncfn, netf;
   unsigned long long t0, tp;

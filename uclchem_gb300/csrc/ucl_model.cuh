@@ -5,8 +5,12 @@
 //   updateChemistry   chemistry.f90:145-239 (retries, stall detector)
 //   integrateODESystem chemistry.f90:241-292 (abstol vector, ISTATE recovery)
 //   output rows       io.f90:74-82
+//   collapse physics  collapse.f90:27-115 (initializePhysics, updateTargetTime,
+//                     updatePhysics), in place of cloud.f90's when
+//                     ucl_model_params::collapse is 1-4
 #pragma once
 #include "ucl_bdf.cuh"
+#include "ucl_collapse.cuh"
 
 namespace ucl {
 
@@ -149,6 +153,64 @@ __device__ void write_row(Ctx<T>& C, const SolveIO& io, int mi) {
   __syncthreads();
 }
 
+// initializePhysics of the collapse module, the part after the mode checks
+// (collapse.f90:56-57): density = rhofit(rin, ...) at t = 0 and, for the
+// Bonnor-Ebert modes, the mass inside the parcel (findMassInRadius,
+// 1000-step trapezoid).  All threads call.  (The collapse functions are not
+// inlined, so they leave the register allocation of the solver alone.)
+template <typename T>
+__device__ __noinline__ void collapse_init(Ctx<T>& C) {
+  Shared& sh = *C.sh;
+  ModelState& ms = sh.ms;
+  const int cm = ms.cmode;
+  const double rho0 = col_rho0fit(cm, 0.0, ms.ctmax), r0 = col_r0fit(cm, 0.0, ms.ctmax), a = col_afit(cm, 0.0);
+  double mass = 0.0;
+  if (cm <= 2) mass = col_trapezoid(1, cm, 1000, 0.0, ms.crad / 1000, rho0, r0, a, sh.red);
+  if (threadIdx.x == 0) {
+    sh.S.dens = col_rhofit(cm, sh.P.rin, rho0, r0, a);
+    ms.cmass = mass;
+  }
+  __syncthreads();
+}
+
+// updatePhysics of the collapse module (collapse.f90:76-106) after
+// coreUpdatePhysics: the column density to the cloud edge from the current
+// profile (findcoldens, 1e4-step trapezoid), Av from it, the parcel's new
+// radius and its density.  All threads call.
+template <typename T>
+__device__ __noinline__ void collapse_update(Ctx<T>& C) {
+  Shared& sh = *C.sh;
+  ModelState& ms = sh.ms;
+  const ucl_model_params& P = sh.P;
+  const int cm = ms.cmode;
+  const double t = ms.tyears;
+  const double rho0 = col_rho0fit(cm, t, ms.ctmax), r0 = col_r0fit(cm, t, ms.ctmax), a = col_afit(cm, t);
+  const double size = P.rout - P.rin;
+  double coldens = 0.0;
+  if (size > 0.0) coldens = col_trapezoid(0, cm, 10000, P.rin, size / 10000, rho0, r0, a, sh.red);
+  double rad = ms.crad;
+  __shared__ int s_err;
+  if (threadIdx.x == 0) s_err = 0;
+  __syncthreads();
+  if (cm <= 2) {
+    // the radius enclosing the parcel's initial mass (findNewRadius with r = rout)
+    rad = col_new_radius(cm, ms.cmass, P.rout, rho0, r0, a, reinterpret_cast<double*>(C.lu_smem), &s_err);
+  } else if (threadIdx.x == 0) {
+    // dt = targetTime - currentTime: zero once the chemistry has reached targetTime
+    const double dt = ms.target - ms.t;
+    const double drad = col_vrfit(cm, ms.crad, col_rminfit(cm, t), col_vminfit(cm, t), col_avfit(cm, t)) * dt / cK.PC;
+    rad = ms.crad + drad;
+  }
+  if (threadIdx.x == 0) {
+    ms.coldens = coldens;
+    sh.S.av = P.baseAv + coldens / 1.6e21;
+    if (s_err || !(rad >= 0.0)) ms.flag = UCL_INT_UNRECOVERABLE_ERROR;
+    ms.crad = rad;
+    sh.S.dens = col_rhofit(cm, rad, rho0, r0, a);
+  }
+  __syncthreads();
+}
+
 template <typename T>
 __device__ void run_model(Ctx<T>& C, const SolveIO& io, int mi, const ucl_model_params* params) {
   const int max_rows = io.max_rows;
@@ -189,9 +251,23 @@ __device__ void run_model(Ctx<T>& C, const SolveIO& io, int mi, const ucl_model_
     if (P.points != 1 || (P.ionModel != 'L' && P.ionModel != 'H') ||
         (P.improvedH2CRPDissociation && !P.cosmicRayAttenuation))
       ms.flag = UCL_PHYSICS_INIT_ERROR;
+    // collapse module set-up (collapse.f90:27-58): maxTime and finalTime of
+    // the Bonnor-Ebert modes, the parcel at rout; another mode number is
+    // "unacceptable collapse mode"
+    ms.cmode = P.collapse;
+    ms.ctmax = 0.0;
+    ms.cmass = 0.0;
+    if (P.collapse != 0) {
+      if (P.collapse < 1 || P.collapse > 4) ms.flag = UCL_PHYSICS_INIT_ERROR;
+      if (P.collapse == 1) ms.ctmax = 1.175e6;
+      if (P.collapse == 2) ms.ctmax = 1.855e5;
+      if (P.collapse == 1 || P.collapse == 2) sh.P.finalTime = (double)0.97f * ms.ctmax;
+      ms.crad = 1 * P.rout / (double)(float)P.points;
+    }
   }
   __syncthreads();
   const ucl_model_params& P = sh.P;
+  if (ms.cmode != 0 && ms.flag == 0) collapse_init(C);
   // initial abundances (initializeChemistry, chemistry.f90:57-105)
   for (int i = tid; i < n; i += NT) y[i] = 1.0e-30;
   __syncthreads();
@@ -230,7 +306,8 @@ __device__ void run_model(Ctx<T>& C, const SolveIO& io, int mi, const ucl_model_
     if (tid == 0) {
       const double told = ms.t;
       ms.tyears = ms.t / cK.SECONDS_PER_YEAR;
-      ms.target = target_time(ms.tyears, cK.SECONDS_PER_YEAR);
+      ms.target = ms.cmode ? col_target_time(ms.tyears, cK.SECONDS_PER_YEAR)
+                           : target_time(ms.tyears, cK.SECONDS_PER_YEAR);
       ms.t = told;
       ms.loop = 0;
       ms.orig = ms.target;
@@ -299,6 +376,10 @@ __device__ void run_model(Ctx<T>& C, const SolveIO& io, int mi, const ucl_model_
     }
     __syncthreads();
     if (ms.flag < 0) break;
+    if (ms.cmode != 0) {
+      collapse_update(C);
+      if (ms.flag < 0) break;
+    }
     write_row(C, io, mi);
   }
   if (tid == 0) {

@@ -1,14 +1,16 @@
-"""Python front end mirroring ``uclchem.model`` for the CLOUD model.
+"""Python front end mirroring ``uclchem.model`` for the CLOUD and collapse
+models.
 
-``cloud`` keeps the signature and return layout of the reference's
-``uclchem.model.cloud`` (src/uclchem/model.py:227-316): physics array
-``[rows, points, 8]``, abundance array ``[rows, points, nspec]``, rates,
-``abundanceStart`` and the success flag, with rows trimmed as
-``_array_clean`` does (model.py:158-187).  The solve runs on the GPU through
-the C ABI; there is no CPU path.
+``cloud`` and ``collapse`` keep the signatures and return layout of the
+reference's ``uclchem.model.cloud`` and ``uclchem.model.collapse``
+(src/uclchem/model.py:227-316, 319-426): physics array ``[rows, points, 8]``,
+abundance array ``[rows, points, nspec]``, rates, ``abundanceStart`` and the
+success flag, with rows trimmed as ``_array_clean`` does (model.py:158-187).
+The solve runs on the GPU through the C ABI; there is no CPU path.
 
 ``cloud_grid`` is the batched sibling: many parameter dictionaries in one
-device launch, one persistent CTA per model.
+device launch, one persistent CTA per model, each with the cloud or a
+collapse physics module.
 """
 from __future__ import annotations
 
@@ -23,6 +25,9 @@ from .params import make_param_array, make_params
 TIMEPOINTS = 500
 N_PHYSICAL_PARAMETERS = 8
 PHYSICAL_PARAMETERS = ["Time", "Density", "gasTemp", "dustTemp", "Av", "radfield", "zeta", "dstep"]
+
+# the collapse argument of uclchem.model.collapse (model.py:355)
+COLLAPSE_MODES = {"BE1.1": 1, "BE4": 2, "filament": 3, "ambipolar": 4}
 
 _CTX: Optional[Context] = None
 
@@ -61,10 +66,20 @@ def _start_vectors(ctx: Context, params, starting_chemistry, n: int):
     return out
 
 
+def _collapse_mode(collapse) -> int:
+    if isinstance(collapse, str):
+        if collapse not in COLLAPSE_MODES:
+            raise ValueError("collapse must be one of 'BE1.1', 'BE4', 'filament', or 'ambipolar'")
+        return COLLAPSE_MODES[collapse]
+    return int(collapse)
+
+
 def cloud_grid(param_dicts: Sequence[Optional[dict]], timepoints: int = TIMEPOINTS,
                starting_chemistry=None, precision="mixed", context: Optional[Context] = None,
-               return_rates: bool = False):
-    """Run many static/freefall CLOUD models in one device launch.
+               return_rates: bool = False, collapse=0):
+    """Run many static/freefall CLOUD models in one device launch; with
+    `collapse` (a mode name of COLLAPSE_MODES or its number, or one per
+    model) the models run the collapse physics module instead.
 
     Returns (physics [n, rows, 8], abundances [n, rows, nspec], nrows [n],
     flags [n], stats [n]) with rows = timepoints + 1, and the rates rows
@@ -72,6 +87,10 @@ def cloud_grid(param_dicts: Sequence[Optional[dict]], timepoints: int = TIMEPOIN
     """
     ctx = context or get_context()
     params = make_param_array(param_dicts)
+    modes = collapse if isinstance(collapse, (list, tuple, np.ndarray)) else [collapse] * len(params)
+    if len(modes) != len(params):
+        raise ValueError("one collapse mode per parameter dictionary")
+    params["collapse"] = [_collapse_mode(m) for m in modes]
     start = _start_vectors(ctx, params, starting_chemistry, len(params))
     return ctx.solve_models(params, timepoints + 1, start=start, precision=_precision(precision),
                             rates=return_rates)
@@ -82,6 +101,29 @@ def cloud(param_dict=None, out_species: Optional[List[str]] = None, return_array
           timepoints: int = TIMEPOINTS, precision="mixed"):
     """Single CLOUD model with the reference's calling convention
     (pre_flight_checklist's argument rules, model.py:102-160)."""
+    return _single(0, param_dict, out_species, return_array, return_dataframe, return_rates,
+                   starting_chemistry, timepoints, precision)
+
+
+def collapse(collapse, physics_output, param_dict=None, out_species: Optional[List[str]] = None,
+             return_array: bool = False, return_dataframe: bool = False, return_rates: bool = False,
+             starting_chemistry=None, timepoints: int = TIMEPOINTS, precision="mixed"):
+    """Single collapse model (Priestley et al. 2018) with the reference's
+    calling convention (model.py:319-426): `collapse` is 'BE1.1', 'BE4',
+    'filament' or 'ambipolar'.  The reference's optional per-interval
+    physics file (`physics_output`) is not written by the device path, so
+    it must be None."""
+    mode = _collapse_mode(collapse) if isinstance(collapse, str) else None
+    if mode is None:
+        raise ValueError("collapse must be one of 'BE1.1', 'BE4', 'filament', or 'ambipolar'")
+    if physics_output is not None:
+        raise ValueError("the device path does not write the collapse physics file: pass physics_output=None")
+    return _single(mode, param_dict, out_species, return_array, return_dataframe, return_rates,
+                   starting_chemistry, timepoints, precision)
+
+
+def _single(mode: int, param_dict, out_species, return_array, return_dataframe, return_rates,
+            starting_chemistry, timepoints, precision):
     if starting_chemistry is not None and not (return_array or return_dataframe):
         raise AssertionError("starting_chemistry can only be used with return_array or return_dataframe set to True")
     if return_rates and not (return_array or return_dataframe):
@@ -99,7 +141,7 @@ def cloud(param_dict=None, out_species: Optional[List[str]] = None, return_array
             return None, None, None, None, flag
         return [flag]
     out = cloud_grid([pd], timepoints=timepoints, starting_chemistry=starting_chemistry,
-                     precision=precision, context=ctx, return_rates=return_rates)
+                     precision=precision, context=ctx, return_rates=return_rates, collapse=mode)
     phys, ab, nrows, flags = out[:4]
     n = int(nrows[0])
     flag = int(flags[0])

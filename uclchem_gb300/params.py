@@ -39,7 +39,7 @@ class ModelParams(ctypes.Structure):
         "desorb", "h2desorb", "crdesorb", "uvdesorb", "thermdesorb",
         "ion", "points", "mxstep",
         "enforceChargeConservation", "improvedH2CRPDissociation",
-        "cosmicRayAttenuation", "ionModel",
+        "cosmicRayAttenuation", "ionModel", "collapse", "reserved",
     )]
 
 
@@ -65,6 +65,9 @@ DEFAULTS: Dict[str, float] = {
     "uvdesorb": 1, "thermdesorb": 1, "ion": 2, "points": 1, "mxstep": 10000,
     "enforceChargeConservation": 0, "improvedH2CRPDissociation": 0,
     "cosmicRayAttenuation": 0, "ionModel": ord("L"),
+    # physics module (not a dictionary key: the collapse argument of
+    # model.collapse selects it; 0 = cloud)
+    "collapse": 0, "reserved": 0,
 }
 
 # dictionaryParser keys (lower case) -> struct field (wrap.f90:755-975)
@@ -74,7 +77,8 @@ _KEYMAP["thermdesorb"] = "uvdesorb"        # quirk Q2 (wrap.f90:802-803)
 _IGNORED = {"outspecies", "writestep", "abundsavefile", "abundloadfile", "outputfile",
             "ratefile", "fluxfile", "columnfile", "ntime", "bm0", "instantsublimation",
             "currenttime"}
-_NOT_PARSED = {"mxstep", "enforcechargeconservation"}  # module variables without a dict key
+# module variables and struct fields without a dict key
+_NOT_PARSED = {"mxstep", "enforcechargeconservation", "collapse", "reserved"}
 
 
 class ParameterError(ValueError):
