@@ -1,0 +1,139 @@
+"""Networks other than the default one on the device: the reference's
+small_chemistry network and the default network with
+add_crp_photo_to_grain, as MakeRates writes them and this repository's
+compiler builds them (tests/golden/networks/, made by
+tests/golden/make_networks.py), against the oracle's runs of the same
+models (tests/golden/networks_oracle.npz): a static cloud and a freefall
+stage 1 per network, both precisions, through the C ABI.  Per model: the
+oracle's flag; at every output time both runs wrote, every species above
+1e-14 within the tolerance; the network's invariants conserved.  The two
+networks and the default one also run together in one launch."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, dex_error
+from uclchem_gb300.params import make_param_array
+
+pytestmark = pytest.mark.gpu
+
+NETS = os.path.join(GOLDEN, "networks")
+FIX = os.path.join(GOLDEN, "networks_oracle.npz")
+ROWS = 501
+MODELS = {
+    "small_chemistry": [
+        ("static", {"initialDens": 1e4, "initialTemp": 10.0, "finalTime": 1e6}),
+        ("stage1", {"initialDens": 1e2, "initialTemp": 10.0, "freefall": True, "endAtFinalDensity": True,
+                    "finalDens": 1e5, "finalTime": 5e6}),
+    ],
+    "photo_on_grain": [
+        ("static", {"initialDens": 1e4, "initialTemp": 10.0, "finalTime": 5e6, "finalDens": 1e5,
+                    "abstol_min": 1e-15, "reltol": 1e-5}),
+        ("stage1", {"initialDens": 1e2, "initialTemp": 10.0, "freefall": True, "endAtFinalDensity": True,
+                    "finalDens": 1e5, "finalTime": 5e6, "abstol_min": 1e-15, "reltol": 1e-5}),
+    ],
+}
+# max |dex| against the oracle at the same tolerances: 0.01 at the
+# reference's reltol 1e-8; the photo-on-grain models run at the reltol 1e-5
+# of the reference's own test of that network, where two correct
+# integrations differ by more
+DEX = {"small_chemistry": 0.01, "photo_on_grain": 0.05}
+
+
+def _common_rows(t_a, t_b):
+    ia, ib = [], []
+    j = 0
+    for i, t in enumerate(t_a):
+        while j < len(t_b) and t_b[j] < t * (1 - 1e-12):
+            j += 1
+        if j < len(t_b) and abs(t_b[j] - t) <= 1e-12 * max(t, 1.0):
+            ia.append(i)
+            ib.append(j)
+    return np.array(ia, dtype=int), np.array(ib, dtype=int)
+
+
+@pytest.fixture(scope="module")
+def fx():
+    if not os.path.exists(FIX):
+        pytest.fail(f"fixture missing: {FIX}")
+    return np.load(FIX)
+
+
+def _check(fx, name, mname, net, ph, ab, nr, fl):
+    key = f"{name}/{mname}/"
+    r = int(fx[key + "nrows"])
+    assert fl == int(fx[key + "flag"]) == 0, (name, mname, fl)
+    ot = fx[key + "tyears"][:r]
+    gi, oi = _common_rows(ph[:nr, 0], ot)
+    assert len(gi) >= min(nr, r) - 2, (name, mname, len(gi), nr, r)
+    oab = 10.0 ** (fx[key + "log10_mdex"][oi].astype(np.float64) / 1000.0)
+    d = dex_error(ab[gi, : net.nspec], oab)
+    assert d < DEX[name], (name, mname, d)
+    tot = ab[:nr, : net.nspec] @ net.invariants().T
+    assert np.abs(tot / tot[0] - 1).max() < 1e-10, (name, mname)
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+@pytest.mark.parametrize("name", list(MODELS))
+def test_network_matches_oracle(fx, name, precision):
+    from uclchem_gb300 import _lib, network
+    net = network.Network.load_npz(os.path.join(NETS, name + ".npz"))
+    ctx = _lib.Context(os.path.join(NETS, name + ".uclnet"), device=0)
+    try:
+        assert ctx.nspec == net.nspec
+        params = make_param_array([pd for _, pd in MODELS[name]])
+        ph, ab, nr, fl, st = ctx.solve_models(params, ROWS, precision=precision)
+        for k, (mname, _) in enumerate(MODELS[name]):
+            _check(fx, name, mname, net, ph[k], ab[k], int(nr[k]), int(fl[k]))
+    finally:
+        ctx.close()
+
+
+def test_three_networks_in_one_launch(fx):
+    """The default network, small_chemistry and photo_on_grain in one
+    context and one launch (mixed): each model's rows agree with those of
+    its own network's context (the slots are sized for the largest network;
+    the two contexts may time the LU variants differently, so to rounding)."""
+    import torch
+    from uclchem_gb300 import _lib, network
+    names = ["small_chemistry", "photo_on_grain"]
+    blobs = [network.DEFAULT_BLOB] + [os.path.join(NETS, n + ".uclnet") for n in names]
+    ctx = _lib.Context(blobs, device=0)
+    try:
+        dicts = [{"initialDens": 1e4, "initialTemp": 10.0, "finalTime": 1e5}] + \
+                [MODELS[n][0][1] for n in names]
+        params = make_param_array(dicts)
+        net_of = np.array([0, 1, 2], dtype=np.int32)
+        M, ns = len(dicts), ctx.nspec
+        dev = torch.device("cuda", 0)
+        p_d = torch.from_numpy(params.view(np.uint8).reshape(M, -1).copy()).to(dev)
+        no_d = torch.from_numpy(net_of).to(dev)
+        ph = torch.zeros((M, ROWS, 8), dtype=torch.float64, device=dev)
+        ab = torch.zeros((M, ROWS, ns), dtype=torch.float64, device=dev)
+        nr = torch.zeros(M, dtype=torch.int32, device=dev)
+        fl = torch.zeros(M, dtype=torch.int32, device=dev)
+        st = torch.zeros((M, _lib.STATS_DTYPE.itemsize), dtype=torch.uint8, device=dev)
+        stream = torch.cuda.Stream(device=dev)
+        torch.cuda.synchronize()
+        ctx.solve_models_nets_device(M, no_d.data_ptr(), p_d.data_ptr(), None, ROWS, ph.data_ptr(), ab.data_ptr(),
+                                     nr.data_ptr(), fl.data_ptr(), st.data_ptr(), _lib.PREC_MIXED, 0,
+                                     stream.cuda_stream)
+        stream.synchronize()
+        ph, ab, nr, fl = ph.cpu().numpy(), ab.cpu().numpy(), nr.cpu().numpy(), fl.cpu().numpy()
+    finally:
+        ctx.close()
+    for k, blob in enumerate(blobs):
+        one = _lib.Context(blob, device=0)
+        try:
+            p1, a1, n1, f1, s1 = one.solve_models(params[k:k + 1], ROWS, precision=_lib.PREC_MIXED)
+        finally:
+            one.close()
+        n = int(n1[0])
+        assert fl[k] == f1[0] == 0 and nr[k] == n, (k, fl[k], f1[0], nr[k], n)
+        assert dex_error(ab[k, :n, : one_nspec(blob)], a1[0, :n, : one_nspec(blob)]) < 1e-3, k
+
+
+def one_nspec(blob):
+    from uclchem_gb300 import network
+    return network.Network.load_npz(blob.replace(".uclnet", ".npz")).nspec
