@@ -75,7 +75,11 @@ typedef struct ucl_model_params {
    * 2018): 1 'BE1.1', 2 'BE4', 3 'filament', 4 'ambipolar', the collapse
    * argument of uclchem.model.collapse (model.py:355, wrap.f90:83-152) */
   int32_t collapse;
-  int32_t reserved; /* 0 */
+  /* hot-core physics module (hotcore.f90): the temp_indx 1-6 of
+   * uclchem.model.hot_core (model.py:429-524; the protostar mass 1, 5, 10,
+   * 15, 25, 60 Msun of the temperature ramp), 0 = off */
+  int32_t hotcore;
+  double maxTemperature; /* the ramp's final temperature (K), max_temperature */
 } ucl_model_params;
 
 /* Fill *p with the reference defaults (defaultparameters.f90:18-119). */
@@ -194,11 +198,13 @@ typedef struct ucl_model_stats {
  * UCL_PHYSICS_INIT_ERROR and no rows: ionModel other than 'L'/'H',
  * improvedH2CRPDissociation without cosmicRayAttenuation
  * (physics-core.f90:55-64), a collapse mode other than 0-4
- * (collapse.f90:44-48), and points != 1 (the reference's multi-parcel
+ * (collapse.f90:44-48), a hot-core temp_indx other than 0-6 or hot core
+ * with collapse (hotcore.f90:38-44), and points != 1 (the reference's multi-parcel
  * column density reads coldens(0), outside its array, physics-core.f90:80).
  * With collapse 1-4 the model runs collapse.f90's physics module: its
  * initializePhysics (BE1.1 and BE4 set finalTime to 0.97 of their maxTime),
- * updateTargetTime and updatePhysics between intervals. */
+ * updateTargetTime and updatePhysics between intervals; with hotcore 1-6,
+ * hotcore.f90's temperature ramp (to maxTemperature) and schedule. */
 int ucl_solve_models(ucl_ctx* ctx, int nmodels, const ucl_model_params* params,
                      const double* start, int max_rows, double* phys_out,
                      double* abund_out, int* nrows_out, int* flag_out,

@@ -1883,6 +1883,33 @@ static double find_new_radius(int mode, double mass, double r, double rho0, doub
   return -1.0;
 }
 
+/* The hot-core physics module (hotcore.f90): the temperature ramp of a
+ * protostar of mass index m (tempa 'd' literals, tempb default REAL) and
+ * its output schedule; its sublimation routine does nothing on a
+ * three-phase network (hotcore.f90:82-96). */
+static const double HC_TEMPA[6] = {1.927e-1, 4.8560e-2, 7.8470e-3, 9.6966e-4, 1.706e-4, 4.74e-7};
+static const float HC_TEMPB[6] = {0.5339f, 0.6255f, 0.8395f, 1.085f, 1.289f, 1.98f};
+
+static double hc_target_time(double ty) { /* hotcore.f90:50-66 */
+  if (ty > 1.0e6) return (ty + 1.0e5) * SECONDS_PER_YEAR;
+  if (ty > 1.0e5) return (ty + 1.0e4) * SECONDS_PER_YEAR;
+  if (ty > 1.0e4) return (ty + 1000.0) * SECONDS_PER_YEAR;
+  if (ty > 1000) return (ty + 100.0) * SECONDS_PER_YEAR;
+  if (ty > 100) return (ty + 10.0) * SECONDS_PER_YEAR;
+  if (ty > 0.0) return (ty * 10.0) * SECONDS_PER_YEAR;
+  return SECONDS_PER_YEAR * 1.0e-7;
+}
+
+static double hc_temperature(int m, double T, double t, const ucl_model_params* p, double cloudSize) {
+  /* hotcore.f90:70-79 for dstep = points = 1 */
+  if (!(T < p->maxTemperature)) return T;
+  double g = (cloudSize / (p->rout * PC)) * (double)((float)1 / (float)p->points);
+  g = pow(g, -0.5);
+  T = p->initialTemp + ((HC_TEMPA[m - 1] * pow(t / SECONDS_PER_YEAR, (double)HC_TEMPB[m - 1])) * g);
+  if (T > p->maxTemperature) T = p->maxTemperature;
+  return T;
+}
+
 static double col_target_time(double ty) { /* collapse.f90:60-72 */
   if (ty > 10000) return (ty + 1000.0) * SECONDS_PER_YEAR;
   if (ty > 1000) return (ty + 100.0) * SECONDS_PER_YEAR;
@@ -1926,6 +1953,12 @@ int orc_cloud_rates(const orc_net* n, const ucl_model_params* p, const double* s
     if (cmode <= 2) cmass = find_mass_in_radius(cmode, crad, rho0, r0, a);
     if (!start) m.abund[neq - 1] = c.density;
   }
+  const int hmode = p->hotcore;
+  if (hmode != 0 && (hmode < 1 || hmode > 6 || cmode != 0)) {
+    chem_free(&c); free(m.abund); free(m.abstol);
+    *nrows = 0;
+    return UCL_PHYSICS_INIT_ERROR; /* tempindx out of the six masses */
+  }
   const ucl_model_params* pp = &c.p;
   dv_alloc(&m.dv, neq);
   m.abstol_factor = p->abstol_factor;
@@ -1940,6 +1973,7 @@ int orc_cloud_rates(const orc_net* n, const ucl_model_params* p, const double* s
     double told = m.currentTime;
     m.timeInYears = m.currentTime / SECONDS_PER_YEAR;
     if (cmode) m.targetTime = col_target_time(m.timeInYears);
+    else if (hmode) m.targetTime = hc_target_time(m.timeInYears);
     else update_target_time(&m);
     m.currentTime = told;
     flag = update_chemistry(&m, &c);
@@ -1950,6 +1984,10 @@ int orc_cloud_rates(const orc_net* n, const ucl_model_params* p, const double* s
     c.av = p->baseAv + c.coldens / 1.6e21;
     c.dustTemp = c.gasTemp;
     if (p->cosmicRayAttenuation && p->improvedH2CRPDissociation) c.h2CRPRate = h2_crp_rate(p, c.coldens);
+    if (hmode) { /* the hot-core module's updatePhysics */
+      c.gasTemp = hc_temperature(hmode, c.gasTemp, m.currentTime, p, c.cloudSize);
+      c.dustTemp = c.gasTemp;
+    }
     if (row >= max_rows) { flag = UCL_NOT_ENOUGH_TIMEPOINTS_ERROR; break; }
     if (cmode) {
       /* the collapse module's updatePhysics (collapse.f90:76-106) */

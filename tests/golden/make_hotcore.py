@@ -1,0 +1,63 @@
+"""Generate the hot-core fixture: the oracle (the CPU restatement of the
+reference's rates + GETYDOT + DVODE MF=22 path with the hotcore.f90
+physics module) on two hot-core models of the default network, from the
+reference's default elemental abundances at 1e5 cm^-3 to 1e5 yr:
+temp_indx 3 (10 Msun) with max_temperature 300 K, and temp_indx 5
+(25 Msun) with 200 K.  Stored per model: flag, rows, DVODE counters, output
+times, gas temperature of every row (float64), and every row's log10
+abundances as int16 milli-dex clamped at -16 dex.  The reference's examples
+hold no hot-core output of this network, so this fixture pins the device
+to the oracle's restatement of hotcore.f90.
+Usage: python tests/golden/make_hotcore.py
+"""
+import multiprocessing as mp
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+MODELS = [(3, 300.0), (5, 200.0)]
+PARAMS = {"initialDens": 1e5, "initialTemp": 10.0, "finalTime": 1e5}
+ROWS = 600
+FLOOR_MDEX = -16000
+
+
+def run(model):
+    from oracle.oracle import Oracle
+    from uclchem_gb300.params import make_params
+    p = make_params(PARAMS)
+    p["hotcore"], p["maxTemperature"] = model
+    phys, ab, flag, cnt = Oracle().cloud(p, max_rows=ROWS)
+    q = np.clip(np.round(1000.0 * np.log10(np.maximum(ab, 1e-30))), FLOOR_MDEX, 32000).astype(np.int16)
+    return int(flag), phys, q, cnt
+
+
+def main():
+    with mp.get_context("spawn").Pool(len(MODELS)) as pool:
+        res = pool.map(run, MODELS, chunksize=1)
+    m = len(res)
+    out = {"temp_indx": np.array([a for a, _ in MODELS], dtype=np.int32),
+           "max_temperature": np.array([b for _, b in MODELS]),
+           "flag": np.array([r[0] for r in res], dtype=np.int32),
+           "nrows": np.array([len(r[1]) for r in res], dtype=np.int32),
+           "counters": np.array([r[3] for r in res], dtype=np.int64),
+           "tyears": np.zeros((m, ROWS)), "gas_temp": np.zeros((m, ROWS)),
+           "log10_mdex": np.full((m, ROWS, 335), FLOOR_MDEX, dtype=np.int16)}
+    for k, r in enumerate(res):
+        n = len(r[1])
+        out["tyears"][k, :n] = r[1][:, 0]
+        out["gas_temp"][k, :n] = r[1][:, 2]
+        out["log10_mdex"][k, :n] = r[2]
+    path = os.path.join(HERE, "hotcore_models.npz")
+    np.savez_compressed(path, **out)
+    for k in range(m):
+        print(MODELS[k], out["flag"][k], out["nrows"][k], out["counters"][k][:4])
+    print("wrote", path)
+
+
+if __name__ == "__main__":
+    main()

@@ -8,9 +8,11 @@
 //   collapse physics  collapse.f90:27-115 (initializePhysics, updateTargetTime,
 //                     updatePhysics), in place of cloud.f90's when
 //                     ucl_model_params::collapse is 1-4
+//   hot-core physics  hotcore.f90:22-79 when ucl_model_params::hotcore is 1-6
 #pragma once
 #include "ucl_bdf.cuh"
 #include "ucl_collapse.cuh"
+#include "ucl_hotcore.cuh"
 
 namespace ucl {
 
@@ -264,6 +266,12 @@ __device__ void run_model(Ctx<T>& C, const SolveIO& io, int mi, const ucl_model_
       if (P.collapse == 1 || P.collapse == 2) sh.P.finalTime = (double)0.97f * ms.ctmax;
       ms.crad = 1 * P.rout / (double)(float)P.points;
     }
+    // hot-core module set-up (hotcore.f90:22-45): temp_indx beyond the six
+    // masses is an error; the reference does not check below 1, which would
+    // index outside its tables, so that is rejected too, as is a model with
+    // both modules
+    ms.hmode = P.hotcore;
+    if (P.hotcore != 0 && (P.hotcore < 1 || P.hotcore > 6 || P.collapse != 0)) ms.flag = UCL_PHYSICS_INIT_ERROR;
   }
   __syncthreads();
   const ucl_model_params& P = sh.P;
@@ -306,8 +314,9 @@ __device__ void run_model(Ctx<T>& C, const SolveIO& io, int mi, const ucl_model_
     if (tid == 0) {
       const double told = ms.t;
       ms.tyears = ms.t / cK.SECONDS_PER_YEAR;
-      ms.target = ms.cmode ? col_target_time(ms.tyears, cK.SECONDS_PER_YEAR)
-                           : target_time(ms.tyears, cK.SECONDS_PER_YEAR);
+      ms.target = ms.cmode   ? col_target_time(ms.tyears, cK.SECONDS_PER_YEAR)
+                  : ms.hmode ? hc_target_time(ms.tyears, cK.SECONDS_PER_YEAR)
+                             : target_time(ms.tyears, cK.SECONDS_PER_YEAR);
       ms.t = told;
       ms.loop = 0;
       ms.orig = ms.target;
@@ -371,6 +380,11 @@ __device__ void run_model(Ctx<T>& C, const SolveIO& io, int mi, const ucl_model_
         S.av = P.baseAv + ms.coldens / 1.6e21;
         S.Td = S.T;
         if (P.cosmicRayAttenuation && P.improvedH2CRPDissociation) S.h2crp = h2_crp_rate(P, ms.coldens);
+        if (ms.hmode) {  // the hot-core module's updatePhysics: the temperature ramp
+          S.T = hc_temperature(ms.hmode, S.T, ms.t, P.initialTemp, P.maxTemperature, (P.rout - P.rin) * cK.PC,
+                               P.rout, P.points);
+          S.Td = S.T;
+        }
         if (ms.row >= max_rows) ms.flag = UCL_NOT_ENOUGH_TIMEPOINTS_ERROR;
       }
     }

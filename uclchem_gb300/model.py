@@ -1,16 +1,16 @@
-"""Python front end mirroring ``uclchem.model`` for the CLOUD and collapse
-models.
+"""Python front end mirroring ``uclchem.model`` for the CLOUD, collapse and
+hot-core models.
 
-``cloud`` and ``collapse`` keep the signatures and return layout of the
-reference's ``uclchem.model.cloud`` and ``uclchem.model.collapse``
-(src/uclchem/model.py:227-316, 319-426): physics array ``[rows, points, 8]``,
+``cloud``, ``collapse`` and ``hot_core`` keep the signatures and return
+layout of the reference's ``uclchem.model.cloud``, ``collapse`` and
+``hot_core`` (src/uclchem/model.py:227-316, 319-426, 429-524): physics array ``[rows, points, 8]``,
 abundance array ``[rows, points, nspec]``, rates, ``abundanceStart`` and the
 success flag, with rows trimmed as ``_array_clean`` does (model.py:158-187).
 The solve runs on the GPU through the C ABI; there is no CPU path.
 
 ``cloud_grid`` is the batched sibling: many parameter dictionaries in one
-device launch, one persistent CTA per model, each with the cloud or a
-collapse physics module.
+device launch, one persistent CTA per model, each with the cloud, a
+collapse or the hot-core physics module.
 """
 from __future__ import annotations
 
@@ -76,10 +76,11 @@ def _collapse_mode(collapse) -> int:
 
 def cloud_grid(param_dicts: Sequence[Optional[dict]], timepoints: int = TIMEPOINTS,
                starting_chemistry=None, precision="mixed", context: Optional[Context] = None,
-               return_rates: bool = False, collapse=0):
+               return_rates: bool = False, collapse=0, hot_core=None):
     """Run many static/freefall CLOUD models in one device launch; with
     `collapse` (a mode name of COLLAPSE_MODES or its number, or one per
-    model) the models run the collapse physics module instead.
+    model) the models run the collapse physics module instead, and with
+    `hot_core` = (temp_indx, max_temperature) the hot-core module.
 
     Returns (physics [n, rows, 8], abundances [n, rows, nspec], nrows [n],
     flags [n], stats [n]) with rows = timepoints + 1, and the rates rows
@@ -91,6 +92,9 @@ def cloud_grid(param_dicts: Sequence[Optional[dict]], timepoints: int = TIMEPOIN
     if len(modes) != len(params):
         raise ValueError("one collapse mode per parameter dictionary")
     params["collapse"] = [_collapse_mode(m) for m in modes]
+    if hot_core is not None:
+        params["hotcore"] = int(hot_core[0])
+        params["maxTemperature"] = float(hot_core[1])
     start = _start_vectors(ctx, params, starting_chemistry, len(params))
     return ctx.solve_models(params, timepoints + 1, start=start, precision=_precision(precision),
                             rates=return_rates)
@@ -122,8 +126,19 @@ def collapse(collapse, physics_output, param_dict=None, out_species: Optional[Li
                    starting_chemistry, timepoints, precision)
 
 
+def hot_core(temp_indx, max_temperature, param_dict=None, out_species: Optional[List[str]] = None,
+             return_array: bool = False, return_dataframe: bool = False, return_rates: bool = False,
+             starting_chemistry=None, timepoints: int = TIMEPOINTS, precision="mixed"):
+    """Single hot-core model with the reference's calling convention
+    (model.py:429-524): `temp_indx` 1-6 selects the protostar mass (1, 5,
+    10, 15, 25, 60 Msun) of the temperature ramp, which stops rising at
+    `max_temperature`."""
+    return _single(0, param_dict, out_species, return_array, return_dataframe, return_rates,
+                   starting_chemistry, timepoints, precision, hot_core=(temp_indx, max_temperature))
+
+
 def _single(mode: int, param_dict, out_species, return_array, return_dataframe, return_rates,
-            starting_chemistry, timepoints, precision):
+            starting_chemistry, timepoints, precision, hot_core=None):
     if starting_chemistry is not None and not (return_array or return_dataframe):
         raise AssertionError("starting_chemistry can only be used with return_array or return_dataframe set to True")
     if return_rates and not (return_array or return_dataframe):
@@ -141,7 +156,8 @@ def _single(mode: int, param_dict, out_species, return_array, return_dataframe, 
             return None, None, None, None, flag
         return [flag]
     out = cloud_grid([pd], timepoints=timepoints, starting_chemistry=starting_chemistry,
-                     precision=precision, context=ctx, return_rates=return_rates, collapse=mode)
+                     precision=precision, context=ctx, return_rates=return_rates, collapse=mode,
+                     hot_core=hot_core)
     phys, ab, nrows, flags = out[:4]
     n = int(nrows[0])
     flag = int(flags[0])

@@ -39,8 +39,8 @@ class ModelParams(ctypes.Structure):
         "desorb", "h2desorb", "crdesorb", "uvdesorb", "thermdesorb",
         "ion", "points", "mxstep",
         "enforceChargeConservation", "improvedH2CRPDissociation",
-        "cosmicRayAttenuation", "ionModel", "collapse", "reserved",
-    )]
+        "cosmicRayAttenuation", "ionModel", "collapse", "hotcore",
+    )] + [("maxTemperature", ctypes.c_double)]
 
 
 PARAMS_DTYPE = np.dtype([(n, np.float64 if t is ctypes.c_double else np.int32)
@@ -65,9 +65,10 @@ DEFAULTS: Dict[str, float] = {
     "uvdesorb": 1, "thermdesorb": 1, "ion": 2, "points": 1, "mxstep": 10000,
     "enforceChargeConservation": 0, "improvedH2CRPDissociation": 0,
     "cosmicRayAttenuation": 0, "ionModel": ord("L"),
-    # physics module (not a dictionary key: the collapse argument of
-    # model.collapse selects it; 0 = cloud)
-    "collapse": 0, "reserved": 0,
+    # physics module (not dictionary keys: the collapse argument of
+    # model.collapse, the temp_indx and max_temperature of model.hot_core;
+    # 0 = cloud)
+    "collapse": 0, "hotcore": 0, "maxTemperature": 0.0,
 }
 
 # dictionaryParser keys (lower case) -> struct field (wrap.f90:755-975)
@@ -78,7 +79,7 @@ _IGNORED = {"outspecies", "writestep", "abundsavefile", "abundloadfile", "output
             "ratefile", "fluxfile", "columnfile", "ntime", "bm0", "instantsublimation",
             "currenttime"}
 # module variables and struct fields without a dict key
-_NOT_PARSED = {"mxstep", "enforcechargeconservation", "collapse", "reserved"}
+_NOT_PARSED = {"mxstep", "enforcechargeconservation", "collapse", "hotcore", "maxtemperature"}
 
 
 class ParameterError(ValueError):
