@@ -1,7 +1,7 @@
 """Generate the hot-core fixture: the oracle (the CPU restatement of the
 reference's rates + GETYDOT + DVODE MF=22 path with the hotcore.f90
 physics module) on two hot-core models of the default network, from the
-reference's default elemental abundances at 1e5 cm^-3 to 1e5 yr:
+reference's default elemental abundances at 1e5 cm^-3 to 5e4 yr:
 temp_indx 3 (10 Msun) with max_temperature 300 K, and temp_indx 5
 (25 Msun) with 200 K.  Stored per model: flag, rows, DVODE counters, output
 times, gas temperature of every row (float64), and every row's log10
@@ -21,7 +21,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 MODELS = [(3, 300.0), (5, 200.0)]
-PARAMS = {"initialDens": 1e5, "initialTemp": 10.0, "finalTime": 1e5}
+PARAMS = {"initialDens": 1e5, "initialTemp": 10.0, "finalTime": 5e4}
 ROWS = 600
 FLOOR_MDEX = -16000
 
