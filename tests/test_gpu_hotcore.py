@@ -58,10 +58,12 @@ def fx():
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
 def test_hot_core_matches_oracle(fx, net, precision):
     from uclchem_gb300 import _lib, network
-    m = len(fx["temp_indx"])
+    # the plain-FP64 path runs the first model only (the 25 Msun ramp takes
+    # ~3e5 steps; its mixed run is compared)
+    m = len(fx["temp_indx"]) if precision == 1 else 1
     params = make_param_array([PARAMS] * m)
-    params["hotcore"] = fx["temp_indx"]
-    params["maxTemperature"] = fx["max_temperature"]
+    params["hotcore"] = fx["temp_indx"][:m]
+    params["maxTemperature"] = fx["max_temperature"][:m]
     ctx = _lib.Context(network.DEFAULT_BLOB, device=0)
     try:
         ph, ab, nr, fl, st = ctx.solve_models(params, ROWS, precision=precision)
