@@ -1,7 +1,7 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
-Compiles oracle/ucl_oracle.c into oracle/liboracle.so with gcc.  The oracle
-is the checker for the GPU path; nothing in the product links it.
+Compiles oracle/ucl_oracle.c into oracle/liboracle.so with gcc.  The tests
+check the GPU path against it; nothing in the product links it.
 ``-ffp-contract=off`` keeps results independent of FMA contraction so the
 same inputs give the same bits on the x86 build host and the Arm GPU host.
 """

@@ -3,8 +3,8 @@
  *
  * A plain-C, FP64, single-threaded-per-model restatement of the reference's
  * chemistry hot path, used ONLY by tests/, __graft_entry__.smoke() and the
- * cpu_baseline leg of bench.py as the checker.  Nothing in the product links
- * or calls this file.
+ * cpu_baseline leg of bench.py, to check and time the GPU path against.
+ * Nothing in the product links or calls this file.
  *
  * What it restates (reference paths relative to the UCLCHEM project):
  *   - calculateReactionRates            src/fortran_src/rates.f90:21-378
