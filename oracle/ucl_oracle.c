@@ -1628,6 +1628,7 @@ typedef struct {
   double* abstol;    /* [neq] */
   dv_t dv;
   double currentTime, targetTime, timeInYears, abstol_factor;
+  int failedIntegrationCounter;
   dv_counts cnt;
   int n_retries;
 } model_t;
@@ -1684,8 +1685,7 @@ static int integrate_interval(model_t* m, chem_t* c) {
   return 0;
 }
 
-/* updateChemistry (chemistry.f90:145-239), with the reference's
- * usepostprocess behaviour */
+/* updateChemistry (chemistry.f90:145-239) */
 static int update_chemistry(model_t* m, chem_t* c) {
   const orc_net* n = c->net;
   int loop = 0, flag = 0;
@@ -1699,14 +1699,11 @@ static int update_chemistry(model_t* m, chem_t* c) {
     c->density = m->abund[n->neq - 1];
     loop++;
     if (loop > 1) m->n_retries++;
-    /* usepostprocess: back to the original target (chemistry.f90:219-220) */
-    m->targetTime = orig;
   }
-  /* The loop-count and stalled-target failures (chemistry.f90:224-236) are
-   * skipped: they run only when usepostprocess is false, and the reference
-   * initialises it .true. (postprocess.f90:14) and never clears it.  An
-   * interval whose target is not reached after ten attempts is left as it
-   * stands, and the caller writes its row at the target's time. */
+  if (loop == 10) flag = UCL_INT_TOO_MANY_FAILS_ERROR;
+  if (fabs(orig - m->targetTime) < SP(0.001) * orig) m->failedIntegrationCounter = 0;
+  else m->failedIntegrationCounter++;
+  if (m->failedIntegrationCounter > 10) flag = UCL_INT_TOO_MANY_FAILS_ERROR;
   return flag;
 }
 
@@ -2346,8 +2343,12 @@ int orc_ma_cloud(int n, int m, const int* ra, const int* rb, const double* k, do
         if (md.abund[i] < MIN_ABUND) md.abund[i] = MIN_ABUND;
       loop++;
       if (loop > 1) md.n_retries++;
-      md.targetTime = orig; /* usepostprocess, as update_chemistry */
     }
+    if (flag < 0) break;
+    if (loop == 10) flag = UCL_INT_TOO_MANY_FAILS_ERROR;
+    if (fabs(orig - md.targetTime) < SP(0.001) * orig) md.failedIntegrationCounter = 0;
+    else md.failedIntegrationCounter++;
+    if (md.failedIntegrationCounter > 10) flag = UCL_INT_TOO_MANY_FAILS_ERROR;
     if (flag < 0) break;
     md.timeInYears = md.targetTime / SECONDS_PER_YEAR;
     if (row >= max_rows) { flag = UCL_NOT_ENOUGH_TIMEPOINTS_ERROR; break; }

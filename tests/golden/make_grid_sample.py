@@ -89,18 +89,10 @@ def main():
     dicts = grid_params(4096, seed=SEED, final_time=1e6)
     path = os.path.join(HERE, "grid_sample_1e6yr.npz")
     if args.add_truth:
-        extra = list(args.add_truth)
+        old = dict(np.load(path))
+        extra = [i for i in args.add_truth if i in set(old["index"].tolist()) and i not in set(old["tight_index"].tolist())]
         with mp.get_context("spawn").Pool(min(args.procs, max(1, len(extra)))) as pool:
             res = pool.map(run, [(i, dicts[i], True, ADD_TRUTH_CAP_S) for i in extra], chunksize=1)
-        # the fixture as it stands once the runs are done
-        old = dict(np.load(path))
-        keep = [k for k, i in enumerate(extra)
-                if i in set(old["index"].tolist()) and i not in set(old["tight_index"].tolist())]
-        extra = [extra[k] for k in keep]
-        res = [r for r in res if r[0] in extra]
-        if not extra:
-            print("nothing to append: no such sample point, or its truth run is already there")
-            return
         new = _pack(res, extra)
         for k, v in new.items():
             old["tight_" + k] = np.concatenate([old["tight_" + k], v])

@@ -39,7 +39,7 @@ struct ModelState {
   double ctmax, crad, cmass;  // collapse module: maxTime, parcel radius (pc), mass inside it
   int cmode;                  // 0 cloud, 1-4 collapse modes
   int hmode;                  // 0 off, 1-6 hot-core temperature ramp
-  int flag, row, loop, retries, model, go;
+  int flag, row, loop, fail_count, retries, model, go;
   long long nst, nfe, nje, nlu, nni, ncfn, netf;
   unsigned long long t0, tp;
   unsigned long long ta;       // arrival time of the request (globaltimer ns)

@@ -2,8 +2,7 @@
 //
 //   model set-up      physics-core.f90:42-73, cloud.f90:20-31, chemistry.f90:46-141
 //   interval loop     wrap.f90:657-690 with cloud.f90:39-51 (updateTargetTime)
-//   updateChemistry   chemistry.f90:145-239 (retries to the original target:
-//                     usepostprocess, postprocess.f90:14)
+//   updateChemistry   chemistry.f90:145-239 (retries, stall detector)
 //   integrateODESystem chemistry.f90:241-292 (abstol vector, ISTATE recovery)
 //   output rows       io.f90:74-82
 //   collapse physics  collapse.f90:27-115 (initializePhysics, updateTargetTime,
@@ -240,6 +239,7 @@ __device__ void run_model(Ctx<T>& C, const SolveIO& io, int mi, const ucl_model_
     ms.tyears = 0.0;
     ms.flag = 0;
     ms.row = 0;
+    ms.fail_count = 0;
     ms.retries = 0;
     ms.abstol_factor = P.abstol_factor;
     ms.nst = ms.nfe = ms.nje = ms.nlu = ms.nni = ms.ncfn = ms.netf = 0;
@@ -366,28 +366,27 @@ __device__ void run_model(Ctx<T>& C, const SolveIO& io, int mi, const ucl_model_
         S.dens = y[n - 1];
         ms.loop++;
         if (ms.loop > 1) ms.retries++;
-        // usepostprocess: back to the original target (chemistry.f90:219-220)
-        ms.target = ms.orig;
       }
       __syncthreads();
     }
-    // The loop-count and stalled-target failures of updateChemistry
-    // (chemistry.f90:224-236) run only when usepostprocess is false; the
-    // reference initialises it .true. (postprocess.f90:14) and never clears
-    // it, so an interval whose target is not reached after ten attempts is
-    // left as it stands and its row is written at the target's time.
     if (tid == 0 && ms.flag == 0) {
-      ms.tyears = ms.target / cK.SECONDS_PER_YEAR;
-      ms.coldens = S.cs * S.dens;  // coreUpdatePhysics (physics-core.f90:75-88)
-      S.av = P.baseAv + ms.coldens / 1.6e21;
-      S.Td = S.T;
-      if (P.cosmicRayAttenuation && P.improvedH2CRPDissociation) S.h2crp = h2_crp_rate(P, ms.coldens);
-      if (ms.hmode) {  // the hot-core module's updatePhysics: the temperature ramp
-        S.T = hc_temperature(ms.hmode, S.T, ms.t, P.initialTemp, P.maxTemperature, (P.rout - P.rin) * cK.PC,
-                             P.rout, P.points);
+      if (ms.loop == 10) ms.flag = UCL_INT_TOO_MANY_FAILS_ERROR;
+      if (fabs(ms.orig - ms.target) < (double)0.001f * ms.orig) ms.fail_count = 0;
+      else ms.fail_count++;
+      if (ms.fail_count > 10) ms.flag = UCL_INT_TOO_MANY_FAILS_ERROR;
+      if (ms.flag == 0) {
+        ms.tyears = ms.target / cK.SECONDS_PER_YEAR;
+        ms.coldens = S.cs * S.dens;  // coreUpdatePhysics (physics-core.f90:75-88)
+        S.av = P.baseAv + ms.coldens / 1.6e21;
         S.Td = S.T;
+        if (P.cosmicRayAttenuation && P.improvedH2CRPDissociation) S.h2crp = h2_crp_rate(P, ms.coldens);
+        if (ms.hmode) {  // the hot-core module's updatePhysics: the temperature ramp
+          S.T = hc_temperature(ms.hmode, S.T, ms.t, P.initialTemp, P.maxTemperature, (P.rout - P.rin) * cK.PC,
+                               P.rout, P.points);
+          S.Td = S.T;
+        }
+        if (ms.row >= max_rows) ms.flag = UCL_NOT_ENOUGH_TIMEPOINTS_ERROR;
       }
-      if (ms.row >= max_rows) ms.flag = UCL_NOT_ENOUGH_TIMEPOINTS_ERROR;
     }
     __syncthreads();
     if (ms.flag < 0) break;
