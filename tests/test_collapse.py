@@ -108,3 +108,20 @@ def test_bonnor_ebert_parcels_keep_their_mass(fx):
             m = np.cumsum(0.5 * (g[1:] + g[:-1]) * (SP(0.05) / 1.0e4) * grid ** 2)
             i = int(np.argmax(m >= mass))
             np.testing.assert_allclose(fx["density"][k, r], rho(mode, grid[i], rho0, r0, a), rtol=1e-3)
+
+
+def test_collapse_and_hot_core_arguments_on_the_host():
+    """model.collapse's argument rules (model.py:355-361) are checked before
+    any device work, and the physics-module fields are not dictionary keys
+    (dictionaryParser rejects unknown keys)."""
+    from uclchem_gb300 import model
+    from uclchem_gb300.params import ParameterError, make_params
+    with pytest.raises(ValueError):
+        model.collapse("BE5", None, {})
+    with pytest.raises(ValueError):
+        model.collapse("BE4", "physics.dat", {})
+    for key in ("collapse", "hotcore", "maxTemperature"):
+        with pytest.raises(ParameterError):
+            make_params({key: 1})
+    p = make_params({})
+    assert p["collapse"] == 0 and p["hotcore"] == 0 and p["maxTemperature"] == 0.0
